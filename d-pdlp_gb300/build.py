@@ -1,0 +1,81 @@
+"""Build the solver library in-tree: ``libcupdlpx_gb300.so`` next to this file.
+
+Every CUDA translation unit is compiled for sm_103a only
+(``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked into
+one shared library with the CUDA runtime linked statically, so the library
+depends on nothing but the driver.  Re-running only recompiles sources newer
+than their objects.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libcupdlpx_gb300.so")
+
+SOURCES = ["solver.cu", "precond.cu", "hooks.cu", "api.cpp", "lpgen.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _flags(src: str) -> list[str]:
+    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+         "-I" + os.path.join(ROOT, "include"), "-I" + CSRC] + ARCH
+    if src == "lpgen.cpp":
+        f += ["-Xcompiler", "-ffp-contract=off"]  # bit-identical on x86 and Arm
+    if src.endswith(".cu") or src == "api.cpp":
+        f += ["--expt-relaxed-constexpr"]
+    if src == "api.cpp":
+        f = ["-x", "cu"] + f  # includes the device-side solver header
+    return f
+
+
+def _headers_mtime() -> float:
+    hs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    hs += [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
+    return max(os.path.getmtime(h) for h in hs)
+
+
+def _compile(src: str, hdr_time: float) -> str:
+    out = os.path.join(OBJ, src + ".o")
+    path = os.path.join(CSRC, src)
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(path), hdr_time):
+        return out
+    cmd = [nvcc(), "-c", path, "-o", out] + _flags(src)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    hdr = _headers_mtime()
+    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, hdr), SOURCES))
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-cudart", "static"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print(LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

@@ -1,0 +1,92 @@
+// hooks.cu -- device-level entry points used by the parity tests
+// (declared in include/pdlp_gb300.h).
+#include <string>
+#include <vector>
+
+#include "pdlp_gb300.h"
+#include "solver.cuh"
+
+namespace pdlp {
+
+// y[r] = sum_k a_rk x_k
+struct PlainEpi {
+  using val_t = double;
+  static constexpr int NF = 0;
+  static constexpr unsigned MAXMASK = 0;
+  const double *x;
+  double *y;
+  __device__ bool init() { return true; }
+  __device__ double gather(int j) const { return x[j]; }
+  __device__ void row(int r, double s, double *) const { y[r] = s; }
+};
+
+}  // namespace pdlp
+
+extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *col_ind,
+                             const double *vals, const double *x, double *y, int tile) {
+  using namespace pdlp;
+  if (rows < 0 || cols < 0 || !row_ptr || (tile != 512 && tile != 2048)) return -1;
+  const int nnz = row_ptr[rows];
+  for (int r = 0; r < rows; ++r)
+    if (row_ptr[r] > row_ptr[r + 1]) return -1;
+  for (int k = 0; k < nnz; ++k)
+    if (col_ind[k] < 0 || col_ind[k] >= cols) return -1;
+  std::vector<int4> blk;
+  std::vector<int2> lr;
+  build_plan_host(rows, row_ptr, tile, blk, lr);
+  void *mem = nullptr;
+  try {
+    size_t bytes = ((size_t)rows + 1) * 4 + (size_t)nnz * 12 + (size_t)cols * 8 +
+                   (size_t)rows * 8 + blk.size() * 24 + lr.size() * 12 + 4096;
+    PDLP_CUDA(cudaMalloc(&mem, bytes));
+    char *p = (char *)mem;
+    auto take = [&](size_t b) {
+      char *q = p;
+      p += (b + 255) & ~(size_t)255;
+      return q;
+    };
+    int *dptr = (int *)take(((size_t)rows + 1) * 4);
+    int *dcol = (int *)take((size_t)nnz * 4 + 4);
+    double *dval = (double *)take((size_t)nnz * 8 + 8);
+    double *dx = (double *)take((size_t)cols * 8 + 8);
+    double *dy = (double *)take((size_t)rows * 8 + 8);
+    SpmvPlan plan;
+    plan.rows = rows;
+    plan.nblk = (int)blk.size();
+    plan.nlong = (int)lr.size();
+    plan.tile = tile;
+    plan.blk = (int4 *)take(blk.size() * 16 + 16);
+    plan.lrow = (int2 *)take(lr.size() * 8 + 8);
+    plan.lcnt = (unsigned *)take(lr.size() * 4 + 4);
+    plan.lsum = (double *)take(blk.size() * 8 + 8);
+    PDLP_CUDA(cudaMemcpy(dptr, row_ptr, ((size_t)rows + 1) * 4, cudaMemcpyHostToDevice));
+    if (nnz) {
+      PDLP_CUDA(cudaMemcpy(dcol, col_ind, (size_t)nnz * 4, cudaMemcpyHostToDevice));
+      PDLP_CUDA(cudaMemcpy(dval, vals, (size_t)nnz * 8, cudaMemcpyHostToDevice));
+    }
+    if (cols) PDLP_CUDA(cudaMemcpy(dx, x, (size_t)cols * 8, cudaMemcpyHostToDevice));
+    if (!blk.empty())
+      PDLP_CUDA(cudaMemcpy(plan.blk, blk.data(), blk.size() * 16, cudaMemcpyHostToDevice));
+    if (!lr.empty()) {
+      PDLP_CUDA(cudaMemcpy(plan.lrow, lr.data(), lr.size() * 8, cudaMemcpyHostToDevice));
+      PDLP_CUDA(cudaMemset(plan.lcnt, 0, lr.size() * 4));
+    }
+    PlainEpi e{dx, dy};
+    if (plan.nblk > 0) {
+      if (tile == 2048)
+        spmv_fused<2048, PlainEpi><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan, nullptr,
+                                                            nullptr, e);
+      else
+        spmv_fused<512, PlainEpi><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan, nullptr,
+                                                           nullptr, e);
+      PDLP_LAUNCH_CHECK();
+    }
+    if (rows) PDLP_CUDA(cudaMemcpy(y, dy, (size_t)rows * 8, cudaMemcpyDeviceToHost));
+    cudaFree(mem);
+    return 0;
+  } catch (const std::exception &e) {
+    if (mem) cudaFree(mem);
+    fprintf(stderr, "[cupdlpx-gb300] pdlp_gpu_spmv: %s\n", e.what());
+    return -2;
+  }
+}

@@ -1,0 +1,224 @@
+// spmv.cuh -- row-binned ("CSR-adaptive") sparse matrix-vector product with a
+// fused per-row epilogue.
+//
+// Replaces the reference's cusparseSpMV(CSR_ALG2) calls
+// (src/pdlp_core_op.cu:501-504, :534-537, :671-674, :801-804;
+// src/utils.cu:134-140, :645-653, :750-758) and the elementwise kernel that
+// follows each of them.
+//
+// Layout: the matrix stays in CSR (int32 row_ptr / col, value array).  A plan
+// cuts the rows into thread-block tiles of at most TILE non-zeros:
+//   * light tile : consecutive rows [r0, r1) whose non-zeros fit in TILE; the
+//                  block streams the tile's values and column indices with
+//                  coalesced loads, gathers x, stages the products in shared
+//                  memory and reduces each row with a group of G lanes
+//                  (G = 256 / rows, power of two, at most 32; one whole block
+//                  when the tile holds a single row);
+//   * long row   : a row with more than TILE non-zeros is cut into chunks, one
+//                  block each; the last block to finish (atomic ticket) sums
+//                  the chunk partials in chunk order and runs the epilogue.
+// Every sum has a fixed order for a given plan, so results are bitwise
+// reproducible run to run.  The epilogue of row r runs once, in one thread,
+// and may add to NF per-block reduction fields (sums, or maxima where bit f
+// of Epi::MAXMASK is set); the block writes them to part[f * nblk + block],
+// and long-row contributions to lpart[f * nlong + long_row], for a
+// single-block finaliser to fold in a fixed order.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace pdlp {
+
+constexpr int kMaxRowsPerTile = 1024;
+
+struct SpmvPlan {
+  int rows = 0, nblk = 0, nlong = 0, tile = 0;
+  int4 *blk = nullptr;        // {r0, r1 | -(long_id+1), k0, k1}
+  int2 *lrow = nullptr;       // per long row {first block, chunk count}
+  unsigned *lcnt = nullptr;   // per long row arrival counter (kept at 0)
+  double *lsum = nullptr;     // per block chunk partial (long rows)
+};
+
+// Host: cut rows into tiles.  `ptr` is the host copy of the row pointer.
+inline void build_plan_host(int rows, const int *ptr, int tile,
+                            std::vector<int4> &blk, std::vector<int2> &lrow) {
+  blk.clear();
+  lrow.clear();
+  int r = 0;
+  while (r < rows) {
+    int len = ptr[r + 1] - ptr[r];
+    if (len > tile) {
+      int nch = (len + tile - 1) / tile;
+      int lid = (int)lrow.size();
+      lrow.push_back(make_int2((int)blk.size(), nch));
+      for (int c = 0; c < nch; ++c) {
+        int k0 = ptr[r] + c * tile;
+        int k1 = k0 + tile < ptr[r + 1] ? k0 + tile : ptr[r + 1];
+        blk.push_back(make_int4(r, -(lid + 1), k0, k1));
+      }
+      ++r;
+    } else {
+      int r0 = r, k0 = ptr[r];
+      while (r < rows && (r - r0) < kMaxRowsPerTile && ptr[r + 1] - k0 <= tile) ++r;
+      blk.push_back(make_int4(r0, r, k0, ptr[r]));
+    }
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T ld_stream(const T *p) {
+  return __ldcs(p);  // matrix data is read once per sweep: evict first
+}
+
+template <int NF, unsigned MAXMASK>
+__device__ __forceinline__ void block_reduce_fields(double (&acc)[NF > 0 ? NF : 1],
+                                                    double *red) {
+  if constexpr (NF > 0) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+      acc[f] = ((MAXMASK >> f) & 1u) ? warp_max(acc[f]) : warp_sum(acc[f]);
+    if (lane == 0) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) red[f * 8 + wid] = acc[f];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w)
+          s = ((MAXMASK >> f) & 1u) ? fmax(s, red[f * 8 + w]) : s + red[f * 8 + w];
+        acc[f] = s;
+      }
+    }
+  }
+}
+
+// Epi must provide:
+//   using val_t; static constexpr int NF; static constexpr unsigned MAXMASK;
+//   __device__ bool init();                       // false: skip (uniform)
+//   __device__ double gather(int col) const;      // x[col] (any transform)
+//   __device__ void row(int r, double sum, double *acc) const;
+template <int TILE, class Epi>
+__global__ void __launch_bounds__(kThreads)
+    spmv_fused(const int *__restrict__ ptr, const int *__restrict__ col,
+               const typename Epi::val_t *__restrict__ val, SpmvPlan plan,
+               double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
+  constexpr int NF = Epi::NF;
+  constexpr int IPT = TILE / kThreads;
+  __shared__ double prod[TILE];
+  __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
+  __shared__ int s_last;
+
+  if (!epi.init()) return;
+  const int4 b = plan.blk[blockIdx.x];
+  const int k0 = b.z, len = b.w - b.z;
+  double acc[NF > 0 ? NF : 1];
+#pragma unroll
+  for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
+
+  // Phase 1: coalesced stream of values / columns, gather of x.
+  {
+    int cidx[IPT];
+    double v[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+      int i = threadIdx.x + u * kThreads;
+      if (i < len) {
+        cidx[u] = ld_stream(col + k0 + i);
+        v[u] = (double)ld_stream(val + k0 + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+      int i = threadIdx.x + u * kThreads;
+      if (i < len) prod[i] = v[u] * epi.gather(cidx[u]);
+    }
+  }
+  __syncthreads();
+
+  if (b.y >= 0) {
+    const int r0 = b.x, R = b.y - b.x;
+    if (R == 1) {
+      double s = 0.0;
+      for (int i = threadIdx.x; i < len; i += kThreads) s += prod[i];
+      double t[1] = {s};
+      block_sum<1>(t, red);
+      if (threadIdx.x == 0) epi.row(r0, t[0], acc);
+    } else {
+      int g = kThreads / (R > 0 ? R : 1);
+      int G = 1;
+      while (G * 2 <= g && G < 32) G *= 2;
+      if (G == 1) {
+        for (int r = r0 + threadIdx.x; r < b.y; r += kThreads) {
+          int beg = ptr[r] - k0, end = ptr[r + 1] - k0;
+          double s = 0.0;
+          for (int i = beg; i < end; ++i) s += prod[i];
+          epi.row(r, s, acc);
+        }
+      } else {
+        int grp = threadIdx.x / G, li = threadIdx.x & (G - 1);
+        int r = r0 + grp;
+        double s = 0.0;
+        if (grp < R) {
+          int beg = ptr[r] - k0, end = ptr[r + 1] - k0;
+          for (int i = beg + li; i < end; i += G) s += prod[i];
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (li == 0 && grp < R) epi.row(r, s, acc);
+      }
+    }
+  } else {
+    // chunk of a long row
+    double s = 0.0;
+    for (int i = threadIdx.x; i < len; i += kThreads) s += prod[i];
+    double t[1] = {s};
+    block_sum<1>(t, red);
+    const int lid = -b.y - 1;
+    if (threadIdx.x == 0) {
+      plan.lsum[blockIdx.x] = t[0];
+      __threadfence();
+      unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
+      s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      const int2 L = plan.lrow[lid];
+      double tot = 0.0;
+      for (int c = 0; c < L.y; ++c) tot += __ldcg(plan.lsum + L.x + c);
+      double lacc[NF > 0 ? NF : 1];
+#pragma unroll
+      for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
+      epi.row(b.x, tot, lacc);
+      if constexpr (NF > 0) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
+      }
+      plan.lcnt[lid] = 0u;  // ready for the next launch
+    }
+  }
+
+  if constexpr (NF > 0) {
+    block_reduce_fields<NF, Epi::MAXMASK>(acc, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) part[f * plan.nblk + blockIdx.x] = acc[f];
+    }
+  }
+}
+
+// Fold per-block and long-row partials of field f of one SpMV site.
+template <bool IS_MAX>
+__device__ double fold_site(const double *part, int nblk, const double *lpart,
+                            int nlong, int f, double *smem) {
+  double a = block_fold<IS_MAX>(part + (long)f * nblk, nblk, smem);
+  double b = block_fold<IS_MAX>(lpart + (long)f * nlong, nlong, smem);
+  return IS_MAX ? fmax(a, b) : a + b;
+}
+
+}  // namespace pdlp

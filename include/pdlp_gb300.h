@@ -1,0 +1,98 @@
+/*
+ * pdlp_gb300.h -- additions of the GB300 solver beyond the reference C API.
+ *
+ * Nothing here replaces a reference entry point; these are new, namespaced
+ * functions (diagnostics, seeded problem generators, and the device-level
+ * hooks the parity tests call).  All take plain host pointers and sizes.
+ * Errors: functions returning int give 0 on success and a negative code on
+ * failure; pdlp_last_error() then describes the failure of the calling thread.
+ */
+#ifndef PDLP_GB300_H
+#define PDLP_GB300_H
+
+#include "cupdlpx_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Diagnostics of one solve. */
+typedef struct {
+  int power_iterations;       /* iterations of the step-size power method */
+  double sigma_max;           /* estimated largest singular value of scaled A */
+  double setup_seconds;       /* upload + transpose + plans + GPU rescaling */
+  double rescale_seconds;     /* GPU rescaling alone */
+  double power_seconds;       /* power method */
+  double loop_seconds;        /* PDHG loop, wall clock */
+  double total_seconds;       /* whole solve_lp_problem call */
+  int graphs;                 /* distinct iteration-chunk CUDA graphs */
+  long long kernel_launches;  /* kernels launched by the solve */
+} pdlp_solve_info_t;
+
+/* Number of doubles per trace record written by pdlp_solve_ex: iteration,
+ * rel. primal residual, rel. dual residual, rel. gap, primal objective,
+ * dual objective, primal weight, fixed-point error, step size, inner count. */
+#define PDLP_TRACE_WIDTH 10
+
+/* solve_lp_problem plus optional per-evaluation trace and diagnostics
+ * (trace/info may be NULL).  Same result ownership as solve_lp_problem. */
+cupdlpx_result_t *pdlp_solve_ex(const lp_problem_t *prob,
+                                const pdhg_parameters_t *params, double *trace,
+                                int trace_cap, int *trace_len,
+                                pdlp_solve_info_t *info);
+
+/* Message of the last failure in this thread ("" if none). */
+const char *pdlp_last_error(void);
+
+/* Name of a termination reason (reference src/utils.cu:173-194). */
+const char *pdlp_termination_reason_to_string(termination_reason_t reason);
+
+/* ---- seeded synthetic LPs (SplitMix64 streams; identical on every host).
+ * All return a problem owned by the caller (lp_problem_free), or NULL. */
+
+/* Uniform random positions (distinct), values N(0,1); x0 ~ U[0,1]^n feasible;
+ * 30% of rows equality l = u = A x0, the rest l = A x0 - U[0,1], u = +inf;
+ * 0 <= x <= 10; c ~ U[-1,1]. */
+lp_problem_t *pdlp_generate_random_lp(int m, int n, long long nnz,
+                                      unsigned long long seed);
+
+/* As above, but column degrees follow a rank Zipf law d_r = max(1, min(cap,
+ * round(C r^-s))) with C chosen so the degrees sum to about nnz_target,
+ * assigned to a random column permutation; rows uniform within a column;
+ * values N(0,1) with 5% of entries +-1. */
+lp_problem_t *pdlp_generate_powerlaw_lp(int m, int n, long long nnz_target,
+                                        double zipf_s, int max_degree,
+                                        unsigned long long seed);
+
+/* Balanced transportation LP: sources x sinks arcs, one equality row per
+ * source (supply ~ U[1,100]) and per sink (demand ~ U[1,100] rescaled to
+ * the total supply), costs ~ U[0,1], x >= 0. */
+lp_problem_t *pdlp_generate_transport_lp(int sources, int sinks,
+                                         unsigned long long seed);
+
+/* ---- device-level hooks (inputs and outputs in host memory) ----------- */
+
+/* GPU rescaling of prob (upload, transpose, Ruiz/PC/bound-objective) with
+ * the scaled problem copied back.  Output sizes: vals nnz, c/lv/uv/var n,
+ * lc/uc/con m. */
+int pdlp_gpu_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params,
+                     double *vals, double *c, double *lv, double *uv,
+                     double *lc, double *uc, double *con_rescale,
+                     double *var_rescale, double *con_bound_rescale,
+                     double *obj_vec_rescale);
+
+/* y = A x with the fused SpMV kernel and a plan of the given tile
+ * (512 or 2048 non-zeros per thread block). */
+int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *col_ind,
+                  const double *vals, const double *x, double *y, int tile);
+
+/* Power method of the solver on the scaled problem of prob; returns the
+ * step-size estimate sigma_max and the iteration count. */
+int pdlp_gpu_power_method(const lp_problem_t *prob,
+                          const pdhg_parameters_t *params, double *sigma_max,
+                          int *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

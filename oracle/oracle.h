@@ -1,0 +1,90 @@
+/*
+ * oracle.h -- CPU FP64 restatement of the reference's single-GPU PDHG solve.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness checker for the
+ * CUDA solver and the timed CPU baseline; the product never links, loads or
+ * calls it.  Each function cites the reference code (D-PDLP, path:line) that
+ * it restates.
+ */
+#ifndef PDLP_ORACLE_H
+#define PDLP_ORACLE_H
+
+#include "cupdlpx_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One record per evaluation iteration, in this order. */
+enum {
+  ORACLE_TR_ITER = 0,
+  ORACLE_TR_REL_PRIMAL,
+  ORACLE_TR_REL_DUAL,
+  ORACLE_TR_REL_GAP,
+  ORACLE_TR_PRIMAL_OBJ,
+  ORACLE_TR_DUAL_OBJ,
+  ORACLE_TR_PRIMAL_WEIGHT,
+  ORACLE_TR_FIXED_POINT_ERROR,
+  ORACLE_TR_STEP_SIZE,
+  ORACLE_TR_INNER_COUNT,
+  ORACLE_TR_WIDTH
+};
+
+/* Full solve: rescale -> power method -> restarted Halpern PDHG -> unscale
+ * (reference src/solver.cu:32-127 with presolve off).  nthreads <= 0 uses
+ * every OpenMP thread.  trace (may be NULL) receives up to trace_cap records
+ * of ORACLE_TR_WIDTH doubles; *trace_len the number written.  The result is
+ * released with oracle_result_free. */
+cupdlpx_result_t *oracle_solve(const lp_problem_t *prob,
+                               const pdhg_parameters_t *params, int nthreads,
+                               double *trace, int trace_cap, int *trace_len);
+void oracle_result_free(cupdlpx_result_t *r);
+
+/* Defaults (reference src/utils.cu:295-329). */
+void oracle_default_parameters(pdhg_parameters_t *p);
+
+/* Rescaling (reference src/preconditioner.c:197-273).  Outputs are caller
+ * buffers: scaled CSR values (nnz), c (n), lv, uv (n), lc, uc (m),
+ * con_rescale (m), var_rescale (n), and the two scalars. */
+void oracle_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params,
+                    double *vals, double *c, double *lv, double *uv,
+                    double *lc, double *uc, double *con_rescale,
+                    double *var_rescale, double *con_bound_rescale,
+                    double *obj_vec_rescale);
+
+/* Stable CSR transpose (what cusparseCsr2cscEx2 produces in
+ * src/pdlp_core_op.cu:109-130): rows of A^T sorted by original row. */
+void oracle_transpose(int m, int n, const int *ap, const int *aj,
+                      const double *ax, int *tp, int *tj, double *tx);
+
+/* y = A x, one sequential sum per row in CSR order. */
+void oracle_spmv(int rows, const int *ap, const int *aj, const double *ax,
+                 const double *x, double *y, int nthreads);
+
+/* Power method on A A^T (reference src/utils.cu:66-171) started from the
+ * given vector v0 (length m).  Returns sigma_max; *iters_out the number of
+ * iterations run. */
+double oracle_power_method(int m, int n, const int *ap, const int *aj,
+                           const double *ax, const double *v0, int max_iter,
+                           double tol, int *iters_out, int nthreads);
+
+/* Start vector of the reference power method: m draws of N(0,1) from a
+ * fresh std::mt19937(1) (reference src/utils.cu:29-30, :79-82). */
+void oracle_power_start_vector(int m, double *v);
+
+/* Format converters (reference src/utils.cu:826-1013).  Output arrays are
+ * malloc'ed and freed by the caller with free().  Return 0 on success. */
+int oracle_dense_to_csr(const matrix_desc_t *d, int **rp, int **ci,
+                        double **v, int *nnz);
+int oracle_csc_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v,
+                      int *nnz);
+int oracle_coo_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v,
+                      int *nnz);
+
+/* Evaluation cadence (reference src/utils.cu:492-501). */
+int oracle_print_frequency(int iter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
