@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <chrono>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -19,6 +20,10 @@
 #include "cupdlpx.h"
 #include "pdlp_gb300.h"
 #include "solver.cuh"
+
+struct pdlp_device_problem {
+  std::unique_ptr<pdlp::DevProblem> P;
+};
 
 namespace {
 
@@ -228,6 +233,70 @@ struct StreamGuard {
   }
 };
 
+cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &p,
+                            cudaStream_t st, double *trace, int trace_cap, int *trace_len,
+                            pdlp_solve_info_t *info,
+                            std::chrono::steady_clock::time_point t0) {
+  pdlp::Solve s(p, st, P, trace ? trace_cap : 0);
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (info) {
+    PDLP_CUDA(cudaEventCreate(&ev0));
+    PDLP_CUDA(cudaEventCreate(&ev1));
+    PDLP_CUDA(cudaEventRecord(ev0, st));
+  }
+  s.prepare();
+  auto t1 = std::chrono::steady_clock::now();
+  s.init_step();
+  auto t2 = std::chrono::steady_clock::now();
+  s.run();
+  cupdlpx_result_t *r = s.result();
+  auto t3 = std::chrono::steady_clock::now();
+  if (info) {
+    PDLP_CUDA(cudaEventRecord(ev1, st));
+    PDLP_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    PDLP_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    info->device_seconds = ms * 1e-3;
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+  }
+  if (trace && trace_len) {
+    std::vector<double> tr = s.trace();
+    int len = (int)(tr.size() / PDLP_TRACE_WIDTH);
+    if (len > trace_cap) len = trace_cap;
+    memcpy(trace, tr.data(), (size_t)len * PDLP_TRACE_WIDTH * sizeof(double));
+    *trace_len = len;
+  }
+  if (info) {
+    info->power_iterations = s.power_iterations();
+    info->sigma_max = s.sigma_max();
+    info->setup_seconds = std::chrono::duration<double>(t1 - t0).count();
+    info->rescale_seconds = s.rescale_seconds();
+    info->power_seconds = std::chrono::duration<double>(t2 - t1).count();
+    info->loop_seconds = s.loop_seconds();
+    info->total_seconds = std::chrono::duration<double>(t3 - t0).count();
+    info->graphs = s.graph_count();
+    info->kernel_launches = s.kernel_launches();
+  }
+  return r;
+}
+
+bool prepare_params(const pdhg_parameters_t *params, pdhg_parameters_t &p) {
+  if (params) p = *params;
+  else set_default_parameters(&p);
+  if (p.termination_evaluation_frequency <= 0) {
+    set_error("solve: termination_evaluation_frequency must be positive.");
+    return false;
+  }
+  if (p.presolve)
+    std::call_once(g_presolve_notice, [] {
+      fprintf(stderr,
+              "[cupdlpx-gb300] presolve requested: this build has no presolver; "
+              "solving the original problem.\n");
+    });
+  return true;
+}
+
 cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *params,
                              double *trace, int trace_cap, int *trace_len,
                              pdlp_solve_info_t *info) {
@@ -236,48 +305,13 @@ cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *
     return nullptr;
   }
   pdhg_parameters_t p;
-  if (params) p = *params;
-  else set_default_parameters(&p);
-  if (p.termination_evaluation_frequency <= 0) {
-    set_error("solve_lp_problem: termination_evaluation_frequency must be positive.");
-    return nullptr;
-  }
-  if (p.presolve)
-    std::call_once(g_presolve_notice, [] {
-      fprintf(stderr,
-              "[cupdlpx-gb300] presolve requested: this build has no presolver; "
-              "solving the original problem.\n");
-    });
+  if (!prepare_params(params, p)) return nullptr;
   auto t0 = std::chrono::steady_clock::now();
   try {
     print_initial_info(&p, prob);
     StreamGuard sg;
-    pdlp::Solve s(p, sg.s, trace ? trace_cap : 0);
-    s.load(prob);
-    auto t1 = std::chrono::steady_clock::now();
-    s.init_step();
-    auto t2 = std::chrono::steady_clock::now();
-    s.run();
-    cupdlpx_result_t *r = s.result(prob);
-    auto t3 = std::chrono::steady_clock::now();
-    if (trace && trace_len) {
-      std::vector<double> tr = s.trace();
-      int len = (int)(tr.size() / PDLP_TRACE_WIDTH);
-      if (len > trace_cap) len = trace_cap;
-      memcpy(trace, tr.data(), (size_t)len * PDLP_TRACE_WIDTH * sizeof(double));
-      *trace_len = len;
-    }
-    if (info) {
-      info->power_iterations = s.power_iterations();
-      info->sigma_max = s.sigma_max();
-      info->setup_seconds = std::chrono::duration<double>(t1 - t0).count();
-      info->rescale_seconds = s.rescale_seconds();
-      info->power_seconds = std::chrono::duration<double>(t2 - t1).count();
-      info->loop_seconds = s.loop_seconds();
-      info->total_seconds = std::chrono::duration<double>(t3 - t0).count();
-      info->graphs = s.graph_count();
-      info->kernel_launches = s.kernel_launches();
-    }
+    std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
+    cupdlpx_result_t *r = run_solve(*P, p, sg.s, trace, trace_cap, trace_len, info, t0);
     if (!quiet_summary()) final_log(r, &p);
     return r;
   } catch (const std::exception &e) {
@@ -463,8 +497,9 @@ int pdlp_gpu_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params, 
   if (!prob || !params) return -1;
   try {
     StreamGuard sg;
-    pdlp::Solve s(*params, sg.s, 0);
-    s.load(prob);
+    std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
+    pdlp::Solve s(*params, sg.s, *P, 0);
+    s.prepare();
     const pdlp::Dev &d = s.dev();
     const int n = d.n, m = d.m, nnz = s.A().nnz;
     auto get = [&](double *dst, const double *src, int cnt) {
@@ -492,14 +527,80 @@ int pdlp_gpu_power_method(const lp_problem_t *prob, const pdhg_parameters_t *par
   if (!prob || !params) return -1;
   try {
     StreamGuard sg;
-    pdlp::Solve s(*params, sg.s, 0);
-    s.load(prob);
+    std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
+    pdlp::Solve s(*params, sg.s, *P, 0);
+    s.prepare();
     s.init_step();
     *sigma_max = s.sigma_max();
     *iterations = s.power_iterations();
     return 0;
   } catch (const std::exception &e) {
     set_error(std::string("pdlp_gpu_power_method: ") + e.what());
+    return -2;
+  }
+}
+
+pdlp_device_problem_t *pdlp_device_problem_create(const lp_problem_t *prob) {
+  if (!prob) {
+    set_error("pdlp_device_problem_create: NULL problem.");
+    return nullptr;
+  }
+  try {
+    StreamGuard sg;
+    auto *dp = new pdlp_device_problem;
+    dp->P.reset(pdlp::upload_problem(prob, sg.s));
+    return dp;
+  } catch (const std::exception &e) {
+    set_error(std::string("pdlp_device_problem_create: ") + e.what());
+    cudaGetLastError();
+    return nullptr;
+  }
+}
+
+void pdlp_device_problem_free(pdlp_device_problem_t *dp) { delete dp; }
+
+long long pdlp_device_problem_bytes(const pdlp_device_problem_t *dp) {
+  return dp && dp->P ? (long long)dp->P->bytes : 0;
+}
+
+cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
+                                            const pdhg_parameters_t *params,
+                                            pdlp_solve_info_t *info) {
+  if (!dp || !dp->P) {
+    set_error("pdlp_device_problem_solve: NULL handle.");
+    return nullptr;
+  }
+  if (info) memset(info, 0, sizeof(*info));
+  pdhg_parameters_t p;
+  if (!prepare_params(params, p)) return nullptr;
+  auto t0 = std::chrono::steady_clock::now();
+  try {
+    StreamGuard sg;
+    cupdlpx_result_t *r = run_solve(*dp->P, p, sg.s, nullptr, 0, nullptr, info, t0);
+    if (!quiet_summary()) final_log(r, &p);
+    return r;
+  } catch (const std::exception &e) {
+    set_error(std::string("pdlp_device_problem_solve: ") + e.what());
+    cudaGetLastError();
+    return nullptr;
+  }
+}
+
+int pdlp_device_problem_time_kernels(pdlp_device_problem_t *dp, const pdhg_parameters_t *params,
+                                     int reps, double *ms) {
+  if (!dp || !dp->P || !ms || reps <= 0) return -1;
+  pdhg_parameters_t p;
+  if (!prepare_params(params, p)) return -1;
+  try {
+    StreamGuard sg;
+    pdlp::Solve s(p, sg.s, *dp->P, 0);
+    s.prepare();
+    s.init_step();
+    s.time_kernels(reps, ms);
+    return 0;
+  } catch (const std::exception &e) {
+    set_error(std::string("pdlp_device_problem_time_kernels: ") + e.what());
+    cudaGetLastError();
     return -2;
   }
 }

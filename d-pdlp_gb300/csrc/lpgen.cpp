@@ -36,7 +36,7 @@ const double kLn2Hi = 6.93147180369123816490e-01;
 const double kLn2Lo = 1.90821492927058770002e-10;
 
 // ln(x), x > 0 finite: x = f 2^e with f in [sqrt(1/2), sqrt(2)),
-// ln f = 2 atanh(z), z = (f-1)/(f+1), odd series to z^41.
+// ln f = 2 atanh(z), z = (f-1)/(f+1), odd series to z^31 (|z| <= 0.1716).
 double det_log(double x) {
   int e;
   double f = frexp(x, &e);  // f in [0.5, 1)
@@ -47,7 +47,7 @@ double det_log(double x) {
   double z = (f - 1.0) / (f + 1.0);
   double z2 = z * z;
   double term = z, s = 0.0;
-  for (int k = 1; k <= 41; k += 2) {
+  for (int k = 1; k <= 31; k += 2) {
     s += term / k;
     term *= z2;
   }
@@ -216,21 +216,22 @@ lp_problem_t *pdlp_generate_powerlaw_lp(int m, int n, long long nnz_target, doub
   ri.reserve((size_t)total);
   ci.reserve((size_t)total);
   v.reserve((size_t)total);
-  std::unordered_set<int> rows;
+  // distinct rows per column: stamp[r] == j marks row r as taken by column j
+  std::vector<int> stamp((size_t)m, -1);
   for (int j = 0; j < n; ++j) {
-    rows.clear();
-    int d = col_deg[j];
-    while ((int)rows.size() < d) {
+    int d = col_deg[j], got = 0;
+    while (got < d) {
       int r = (int)rng.below((uint64_t)m);
-      if (rows.insert(r).second) {
-        ri.push_back(r);
-        ci.push_back(j);
-        double u = rng.uniform();
-        double val;
-        if (u < 0.05) val = (rng.next() & 1) ? 1.0 : -1.0;
-        else val = rng.normal();
-        v.push_back(val);
-      }
+      if (stamp[r] == j) continue;
+      stamp[r] = j;
+      ++got;
+      ri.push_back(r);
+      ci.push_back(j);
+      double u = rng.uniform();
+      double val;
+      if (u < 0.05) val = (rng.next() & 1) ? 1.0 : -1.0;
+      else val = rng.normal();
+      v.push_back(val);
     }
   }
   lp_problem_t *p = alloc_problem(m, n, (long)total);

@@ -628,6 +628,11 @@ struct Arena {
     return p;
   }
 };
+
+struct Sizer {
+  size_t bytes = 0;
+  void add(size_t b) { bytes += align256(b + 1); }
+};
 }  // namespace
 
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
@@ -648,27 +653,21 @@ void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax
     }
 }
 
-Solve::Solve(const pdhg_parameters_t &params, cudaStream_t stream, int trace_cap)
-    : p_(params), st_(stream), trace_cap_(trace_cap) {}
-
-Solve::~Solve() {
-  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
-  for (auto g : raw_graphs_) cudaGraphDestroy(g);
-  if (arena_) cudaFree(arena_);
-  if (hflag_) cudaFreeHost(hflag_);
-}
-
 static int pick_tile(long nnz) { return nnz >= 2000000 ? 2048 : 512; }
 
-void Solve::alloc(const lp_problem_t *prob) {
+DevProblem::~DevProblem() {
+  if (arena) cudaFree(arena);
+}
+
+DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   const int n = prob->num_variables, m = prob->num_constraints;
   const int nnz = prob->constraint_matrix_num_nonzeros;
-  const int tile = pick_tile(nnz);
   // A malformed CSR must never reach the host transpose or a device gather.
   {
     const int *rp = prob->constraint_matrix_row_pointers;
     const int *cj = prob->constraint_matrix_col_indices;
-    bool ok = n >= 0 && m >= 0 && nnz >= 0 && rp && (nnz == 0 || (cj && prob->constraint_matrix_values)) &&
+    bool ok = n >= 0 && m >= 0 && nnz >= 0 && rp &&
+              (nnz == 0 || (cj && prob->constraint_matrix_values)) &&
               (n == 0 || (prob->objective_vector && prob->variable_lower_bound &&
                           prob->variable_upper_bound)) &&
               (m == 0 || (prob->constraint_lower_bound && prob->constraint_upper_bound));
@@ -677,75 +676,167 @@ void Solve::alloc(const lp_problem_t *prob) {
     for (int k = 0; ok && k < nnz; ++k) ok = cj[k] >= 0 && cj[k] < n;
     if (!ok) throw std::runtime_error("invalid CSR matrix (row pointers or column indices)");
   }
-  // plans from the host row pointers
-  std::vector<int4> blkA, blkT;
-  std::vector<int2> lrA, lrT;
+  auto P = std::make_unique<DevProblem>();
+  P->m = m;
+  P->n = n;
+  P->nnz = nnz;
+  P->tile = pick_tile(nnz);
+  P->c0 = prob->objective_constant;
   std::vector<int> tp, tj;
   std::vector<double> tx;
-  host_transpose(m, n, prob->constraint_matrix_row_pointers,
-                 prob->constraint_matrix_col_indices, prob->constraint_matrix_values, tp,
-                 tj, tx);
-  build_plan_host(m, prob->constraint_matrix_row_pointers, tile, blkA, lrA);
-  build_plan_host(n, tp.data(), tile, blkT, lrT);
-  const int ew = grid_for((long)n + m, 4);
+  host_transpose(m, n, prob->constraint_matrix_row_pointers, prob->constraint_matrix_col_indices,
+                 prob->constraint_matrix_values, tp, tj, tx);
+  std::vector<int4> blkA, blkT;
+  std::vector<int2> lrA, lrT;
+  build_plan_host(m, prob->constraint_matrix_row_pointers, P->tile, blkA, lrA);
+  build_plan_host(n, tp.data(), P->tile, blkT, lrT);
+  // norms of the unscaled objective and bounds (reference pdlp_core_op.cu:232-286)
+  {
+    double ss = 0, mx = 0;
+    for (int i = 0; i < n; ++i) {
+      double v = prob->objective_vector[i];
+      mx = fmax(mx, fabs(v));
+      ss += v * v;
+    }
+    P->cnorm_l2 = sqrt(ss);
+    P->cnorm_linf = mx;
+    ss = 0;
+    mx = 0;
+    for (int i = 0; i < m; ++i) {
+      double lo = prob->constraint_lower_bound[i], up = prob->constraint_upper_bound[i];
+      if (isfinite(lo) && lo != up) {
+        mx = fmax(mx, fabs(lo));
+        ss += lo * lo;
+      }
+      if (isfinite(up)) {
+        mx = fmax(mx, fabs(up));
+        ss += up * up;
+      }
+    }
+    P->bnorm_l2 = sqrt(ss);
+    P->bnorm_linf = mx;
+  }
+  const size_t vn = n, vm = m;
+  Sizer z;
+  z.add((vm + 1) * 4); z.add((size_t)nnz * 4); z.add((size_t)nnz * 8);
+  z.add((vn + 1) * 4); z.add((size_t)nnz * 4); z.add((size_t)nnz * 8);
+  z.add(blkA.size() * 16); z.add(lrA.size() * 8);
+  z.add(blkT.size() * 16); z.add(lrT.size() * 8);
+  for (int i = 0; i < 3; ++i) z.add(vn * 8);
+  for (int i = 0; i < 2; ++i) z.add(vm * 8);
+  if (prob->primal_start) z.add(vn * 8);
+  if (prob->dual_start) z.add(vm * 8);
+  PDLP_CUDA(cudaMalloc(&P->arena, z.bytes));
+  P->bytes = z.bytes;
+  Arena ar{(char *)P->arena, 0};
+  auto mat = [&](DevCsr &M, int rows, int cols, std::vector<int4> &blk, std::vector<int2> &lr) {
+    M.rows = rows;
+    M.cols = cols;
+    M.nnz = nnz;
+    M.ptr = ar.take<int>((size_t)rows + 1);
+    M.col = ar.take<int>(nnz);
+    M.val = ar.take<double>(nnz);
+    M.plan.rows = rows;
+    M.plan.nblk = (int)blk.size();
+    M.plan.nlong = (int)lr.size();
+    M.plan.tile = P->tile;
+    M.plan.blk = ar.take<int4>(blk.size());
+    M.plan.lrow = ar.take<int2>(lr.size());
+    if (!blk.empty())
+      PDLP_CUDA(cudaMemcpyAsync(M.plan.blk, blk.data(), blk.size() * 16, cudaMemcpyHostToDevice, st));
+    if (!lr.empty())
+      PDLP_CUDA(cudaMemcpyAsync(M.plan.lrow, lr.data(), lr.size() * 8, cudaMemcpyHostToDevice, st));
+  };
+  mat(P->A, m, n, blkA, lrA);
+  mat(P->AT, n, m, blkT, lrT);
+  P->c = ar.take<double>(vn);
+  P->lv = ar.take<double>(vn);
+  P->uv = ar.take<double>(vn);
+  P->lc = ar.take<double>(vm);
+  P->uc = ar.take<double>(vm);
+  auto h2d = [&](void *dst, const void *src, size_t b) {
+    if (b) PDLP_CUDA(cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, st));
+  };
+  h2d(P->A.ptr, prob->constraint_matrix_row_pointers, (vm + 1) * 4);
+  h2d(P->A.col, prob->constraint_matrix_col_indices, (size_t)nnz * 4);
+  h2d(P->A.val, prob->constraint_matrix_values, (size_t)nnz * 8);
+  h2d(P->AT.ptr, tp.data(), (vn + 1) * 4);
+  h2d(P->AT.col, tj.data(), (size_t)nnz * 4);
+  h2d(P->AT.val, tx.data(), (size_t)nnz * 8);
+  h2d(P->c, prob->objective_vector, vn * 8);
+  h2d(P->lv, prob->variable_lower_bound, vn * 8);
+  h2d(P->uv, prob->variable_upper_bound, vn * 8);
+  h2d(P->lc, prob->constraint_lower_bound, vm * 8);
+  h2d(P->uc, prob->constraint_upper_bound, vm * 8);
+  if (prob->primal_start) {
+    P->xs = ar.take<double>(vn);
+    h2d(P->xs, prob->primal_start, vn * 8);
+  }
+  if (prob->dual_start) {
+    P->ys = ar.take<double>(vm);
+    h2d(P->ys, prob->dual_start, vm * 8);
+  }
+  PDLP_CUDA(cudaStreamSynchronize(st));  // host staging (tp/tj/tx) must outlive the copies
+  return P.release();
+}
 
-  size_t vn = (size_t)n, vm = (size_t)m;
-  size_t bytes = 0;
-  auto add = [&](size_t b) { bytes += align256(b + 1); };
-  // matrices
-  add((vm + 1) * 4); add((size_t)nnz * 4); add((size_t)nnz * 8);
-  add((vn + 1) * 4); add((size_t)nnz * 4); add((size_t)nnz * 8);
-  // plans
-  add(blkA.size() * 16); add(lrA.size() * 8); add(lrA.size() * 4); add(blkA.size() * 8);
-  add(blkT.size() * 16); add(lrT.size() * 8); add(lrT.size() * 4); add(blkT.size() * 8);
-  // problem vectors: c lv uv lvf uvf Dc (n) ; lc uc lcf ucf Dr (m)
-  for (int i = 0; i < 6; ++i) add(vn * 8);
-  for (int i = 0; i < 5; ++i) add(vm * 8);
-  // iterates: x[2] x0 xref xhat lam dx auxn (8 n) ; y[2] y0 yhat dy auxm (6 m)
-  for (int i = 0; i < 8; ++i) add(vn * 8);
-  for (int i = 0; i < 6; ++i) add(vm * 8);
-  // power: v[2] (m) g (n)
-  add(vm * 8); add(vm * 8); add(vn * 8);
-  // partials
-  size_t nbA = blkA.size(), nbT = blkT.size(), nlA = lrA.size(), nlT = lrT.size();
+Solve::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
+             int trace_cap)
+    : p_(params), st_(stream), P_(prob), trace_cap_(trace_cap) {
+  alloc();
+}
+
+Solve::~Solve() {
+  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+  for (auto g : raw_graphs_) cudaGraphDestroy(g);
+  if (arena_) cudaFree(arena_);
+  if (hflag_) cudaFreeHost(hflag_);
+}
+
+void Solve::alloc() {
+  const int n = P_.n, m = P_.m, nnz = P_.nnz;
+  const int ew = grid_for((long)n + m, 4);
+  const size_t vn = n, vm = m;
+  const size_t nbA = P_.A.plan.nblk, nbT = P_.AT.plan.nblk;
+  const size_t nlA = P_.A.plan.nlong, nlT = P_.AT.plan.nlong;
+  Sizer z;
+  z.add((size_t)nnz * 8); z.add((size_t)nnz * 8);           // scaled values
+  z.add(nlA * 4); z.add(nbA * 8); z.add(nlT * 4); z.add(nbT * 8);  // per-solve plan scratch
+  for (int i = 0; i < 6; ++i) z.add(vn * 8);  // c lv uv lvf uvf Dc
+  for (int i = 0; i < 5; ++i) z.add(vm * 8);  // lc uc lcf ucf Dr
+  for (int i = 0; i < 8; ++i) z.add(vn * 8);  // x[2] x0 xref xhat lam dx auxn
+  for (int i = 0; i < 6; ++i) z.add(vm * 8);  // y[2] y0 yhat dy auxm
+  z.add(vm * 8); z.add(vm * 8); z.add(vn * 8);  // power v[2], g
   size_t pa = nbA + nlA + 2, pt = nbT + nlT + 2;
-  add(pt * 8 * 1); add(pa * 8 * 1); add(pt * 8 * 1);  // pstep dstep fpe
-  add(pa * 8 * 2); add(pt * 8 * 3);                  // e1 e2
-  add((size_t)ew * 8 * 2);                           // i0
-  add(pa * 8 * 2); add(pt * 8 * 3);                  // i1 i2
-  add((size_t)ew * 8 * 2);                           // rs
-  add(pa * 8 * 2); add((size_t)ew * 8);              // pa pr
-  add((size_t)kMiscPart * 8);                        // misc (rescale)
-  add(sizeof(Ctl)); add((size_t)trace_cap_ * 10 * 8 + 8); add(64);
-  PDLP_CUDA(cudaMalloc(&arena_, bytes));
+  z.add(pt * 8); z.add(pa * 8); z.add(pt * 8);  // pstep dstep fpe
+  z.add(pa * 16); z.add(pt * 24);               // e1 e2
+  z.add((size_t)ew * 16);                       // i0
+  z.add(pa * 16); z.add(pt * 24);               // i1 i2
+  z.add((size_t)ew * 16);                       // rs
+  z.add(pa * 16); z.add((size_t)ew * 8);        // pa pr
+  z.add((size_t)kMiscPart * 8);
+  z.add(sizeof(Ctl)); z.add((size_t)trace_cap_ * 80 + 8);
+  PDLP_CUDA(cudaMalloc(&arena_, z.bytes));
   Arena ar{(char *)arena_, 0};
 
-  A_.rows = m; A_.cols = n; A_.nnz = nnz;
-  AT_.rows = n; AT_.cols = m; AT_.nnz = nnz;
-  A_.ptr = ar.take<int>(vm + 1); A_.col = ar.take<int>(nnz); A_.val = ar.take<double>(nnz);
-  AT_.ptr = ar.take<int>(vn + 1); AT_.col = ar.take<int>(nnz); AT_.val = ar.take<double>(nnz);
-  auto setup_plan = [&](SpmvPlan &P, int rows, std::vector<int4> &blk, std::vector<int2> &lr) {
-    P.rows = rows; P.nblk = (int)blk.size(); P.nlong = (int)lr.size(); P.tile = tile;
-    P.blk = ar.take<int4>(blk.size()); P.lrow = ar.take<int2>(lr.size());
-    P.lcnt = ar.take<unsigned>(lr.size()); P.lsum = ar.take<double>(blk.size());
-    if (!blk.empty())
-      PDLP_CUDA(cudaMemcpyAsync(P.blk, blk.data(), blk.size() * 16, cudaMemcpyHostToDevice, st_));
-    if (!lr.empty()) {
-      PDLP_CUDA(cudaMemcpyAsync(P.lrow, lr.data(), lr.size() * 8, cudaMemcpyHostToDevice, st_));
-      PDLP_CUDA(cudaMemsetAsync(P.lcnt, 0, lr.size() * 4, st_));
-    }
+  auto mat = [&](DevCsr &W, const DevCsr &S) {
+    W = S;
+    W.val = ar.take<double>(nnz);
+    W.plan.lcnt = ar.take<unsigned>(S.plan.nlong);
+    W.plan.lsum = ar.take<double>(S.plan.nblk);
+    if (S.plan.nlong)
+      PDLP_CUDA(cudaMemsetAsync(W.plan.lcnt, 0, (size_t)S.plan.nlong * 4, st_));
   };
-  setup_plan(A_.plan, m, blkA, lrA);
-  setup_plan(AT_.plan, n, blkT, lrT);
+  mat(A_, P_.A);
+  mat(AT_, P_.AT);
 
   Dev &d = d_;
-  d.n = n; d.m = m;
-  double *c = ar.take<double>(vn), *lv = ar.take<double>(vn), *uv = ar.take<double>(vn);
-  double *lvf = ar.take<double>(vn), *uvf = ar.take<double>(vn), *Dc = ar.take<double>(vn);
-  double *lc = ar.take<double>(vm), *uc = ar.take<double>(vm), *lcf = ar.take<double>(vm);
-  double *ucf = ar.take<double>(vm), *Dr = ar.take<double>(vm);
-  d.c = c; d.lv = lv; d.uv = uv; d.lvf = lvf; d.uvf = uvf; d.Dc = Dc;
-  d.lc = lc; d.uc = uc; d.lcf = lcf; d.ucf = ucf; d.Dr = Dr;
+  d.n = n;
+  d.m = m;
+  d.c = ar.take<double>(vn); d.lv = ar.take<double>(vn); d.uv = ar.take<double>(vn);
+  d.lvf = ar.take<double>(vn); d.uvf = ar.take<double>(vn); d.Dc = ar.take<double>(vn);
+  d.lc = ar.take<double>(vm); d.uc = ar.take<double>(vm); d.lcf = ar.take<double>(vm);
+  d.ucf = ar.take<double>(vm); d.Dr = ar.take<double>(vm);
   d.x[0] = ar.take<double>(vn); d.x[1] = ar.take<double>(vn); d.x0 = ar.take<double>(vn);
   d.xref = ar.take<double>(vn); d.xhat = ar.take<double>(vn); d.lam = ar.take<double>(vn);
   d.dx = ar.take<double>(vn); d.auxn = ar.take<double>(vn);
@@ -781,41 +872,18 @@ void Solve::alloc(const lp_problem_t *prob) {
   HostFlag *dflag = nullptr;
   PDLP_CUDA(cudaHostGetDevicePointer((void **)&dflag, hflag_, 0));
   d.hflag = dflag;
-
-  // uploads (host arrays are pageable; copies are stream ordered)
-  PDLP_CUDA(cudaMemcpyAsync(A_.ptr, prob->constraint_matrix_row_pointers, (vm + 1) * 4,
-                            cudaMemcpyHostToDevice, st_));
-  if (nnz) {
-    PDLP_CUDA(cudaMemcpyAsync(A_.col, prob->constraint_matrix_col_indices, (size_t)nnz * 4,
-                              cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(A_.val, prob->constraint_matrix_values, (size_t)nnz * 8,
-                              cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(AT_.col, tj.data(), (size_t)nnz * 4, cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(AT_.val, tx.data(), (size_t)nnz * 8, cudaMemcpyHostToDevice, st_));
-  }
-  PDLP_CUDA(cudaMemcpyAsync(AT_.ptr, tp.data(), (vn + 1) * 4, cudaMemcpyHostToDevice, st_));
-  if (n) {
-    PDLP_CUDA(cudaMemcpyAsync(c, prob->objective_vector, vn * 8, cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(lv, prob->variable_lower_bound, vn * 8, cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(uv, prob->variable_upper_bound, vn * 8, cudaMemcpyHostToDevice, st_));
-  }
-  if (m) {
-    PDLP_CUDA(cudaMemcpyAsync(lc, prob->constraint_lower_bound, vm * 8, cudaMemcpyHostToDevice, st_));
-    PDLP_CUDA(cudaMemcpyAsync(uc, prob->constraint_upper_bound, vm * 8, cudaMemcpyHostToDevice, st_));
-  }
-  PDLP_CUDA(cudaStreamSynchronize(st_));  // keeps tp/tj/tx alive until uploaded
 }
 
-void Solve::load(const lp_problem_t *prob) {
-  alloc(prob);
+void Solve::prepare() {
   Dev &d = d_;
-  const int n = d.n, m = d.m;
+  const int n = d.n, m = d.m, nnz = P_.nnz;
   auto t0 = std::chrono::steady_clock::now();
-  // constants
-  d.c0 = prob->objective_constant;
+  d.c0 = P_.c0;
   d.rho = p_.reflection_coefficient;
   d.F = p_.termination_evaluation_frequency > 0 ? p_.termination_evaluation_frequency : 1;
   d.linf = p_.optimality_norm == NORM_TYPE_L_INF;
+  d.cnorm = d.linf ? P_.cnorm_linf : P_.cnorm_l2;
+  d.bnorm = d.linf ? P_.bnorm_linf : P_.bnorm_l2;
   d.verbose = p_.verbose;
   d.eps_opt = p_.termination_criteria.eps_optimal_relative;
   d.eps_feas = p_.termination_criteria.eps_feasible_relative;
@@ -829,33 +897,16 @@ void Solve::load(const lp_problem_t *prob) {
   d.kd = p_.restart_params.k_d;
   d.ismooth = p_.restart_params.i_smooth;
   d.sv_tol = p_.sv_tol;
-
-  // norms of the unscaled objective and bounds, on the host copy the
-  // caller handed in (reference pdlp_core_op.cu:232-286)
-  {
-    bool linf = d.linf;
-    double ss = 0, mx = 0;
-    for (int i = 0; i < n; ++i) {
-      double v = prob->objective_vector[i];
-      if (linf) mx = fmax(mx, fabs(v));
-      else ss += v * v;
-    }
-    d.cnorm = linf ? mx : sqrt(ss);
-    ss = 0;
-    mx = 0;
-    for (int i = 0; i < m; ++i) {
-      double lo = prob->constraint_lower_bound[i], up = prob->constraint_upper_bound[i];
-      if (linf) {
-        if (isfinite(lo) && lo != up) mx = fmax(mx, fabs(lo));
-        if (isfinite(up)) mx = fmax(mx, fabs(up));
-      } else {
-        if (isfinite(lo) && lo != up) ss += lo * lo;
-        if (isfinite(up)) ss += up * up;
-      }
-    }
-    d.bnorm = linf ? mx : sqrt(ss);
-  }
-
+  auto d2d = [&](const void *dst, const void *src, size_t b) {
+    if (b) PDLP_CUDA(cudaMemcpyAsync((void *)dst, src, b, cudaMemcpyDeviceToDevice, st_));
+  };
+  d2d(A_.val, P_.A.val, (size_t)nnz * 8);
+  d2d(AT_.val, P_.AT.val, (size_t)nnz * 8);
+  d2d(d.c, P_.c, (size_t)n * 8);
+  d2d(d.lv, P_.lv, (size_t)n * 8);
+  d2d(d.uv, P_.uv, (size_t)n * 8);
+  d2d(d.lc, P_.lc, (size_t)m * 8);
+  d2d(d.uc, P_.uc, (size_t)m * 8);
   gpu_rescale(p_, A_, AT_, (double *)d.c, (double *)d.lv, (double *)d.uv, (double *)d.lc,
               (double *)d.uc, (double *)d.Dr, (double *)d.Dc, &d.cb, &d.ob, d.auxn, d.auxm,
               d.p_misc, st_);
@@ -864,23 +915,13 @@ void Solve::load(const lp_problem_t *prob) {
   k_finite_copies<<<g, kThreads, 0, st_>>>(n, m, d.lv, d.uv, d.lc, d.uc, (double *)d.lvf,
                                            (double *)d.uvf, (double *)d.lcf, (double *)d.ucf);
   PDLP_LAUNCH_CHECK();
-  // iterates start at zero
   for (double *p : {d.x[0], d.x[1], d.x0, d.xref, d.xhat, d.lam, d.dx})
     if (n) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)n * 8, st_));
   for (double *p : {d.y[0], d.y[1], d.y0, d.yhat, d.dy})
     if (m) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)m * 8, st_));
-  if (prob->primal_start || prob->dual_start) {
-    double *xs = nullptr, *ys = nullptr;
-    if (prob->primal_start && n) {
-      xs = d.auxn;
-      PDLP_CUDA(cudaMemcpyAsync(xs, prob->primal_start, (size_t)n * 8, cudaMemcpyHostToDevice, st_));
-    }
-    if (prob->dual_start && m) {
-      ys = d.auxm;
-      PDLP_CUDA(cudaMemcpyAsync(ys, prob->dual_start, (size_t)m * 8, cudaMemcpyHostToDevice, st_));
-    }
-    k_warm_start<<<g, kThreads, 0, st_>>>(n, m, xs, ys, d.Dc, d.Dr, d.cb, d.ob, d.x0, d.x[0],
-                                          d.xhat, d.y0, d.y[0], d.yhat);
+  if (P_.xs || P_.ys) {
+    k_warm_start<<<g, kThreads, 0, st_>>>(n, m, P_.xs, P_.ys, d.Dc, d.Dr, d.cb, d.ob, d.x0,
+                                          d.x[0], d.xhat, d.y0, d.y[0], d.yhat);
     PDLP_LAUNCH_CHECK();
   }
   Ctl c0;
@@ -890,6 +931,8 @@ void Solve::load(const lp_problem_t *prob) {
   c0.reason = TERMINATION_REASON_UNSPECIFIED;
   PDLP_CUDA(cudaMemcpyAsync(d.ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
+  hflag_->done = 0;
+  hflag_->pm_done = 0;
 }
 
 void Solve::power_method() {
@@ -1088,6 +1131,31 @@ void Solve::run() {
   loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+void Solve::time_kernels(int reps, double *ms) {
+  Dev &d = d_;
+  cudaEvent_t e0, e1;
+  PDLP_CUDA(cudaEventCreate(&e0));
+  PDLP_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](auto &&launch) {
+    launch();  // warm
+    PDLP_CUDA(cudaEventRecord(e0, st_));
+    for (int i = 0; i < reps; ++i) launch();
+    PDLP_CUDA(cudaEventRecord(e1, st_));
+    PDLP_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    PDLP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    return (double)t / reps;
+  };
+  PrimalEpi<false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], 0.0, 0.0};
+  DualEpi<false, false> de{d, 0, d.y[0], d.y[1], 0.0, 0.0};
+  ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
+  ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
+  ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<false>{d}, d.p_e1, d.lp_e1, st_); });
+  ms[3] = timed([&] { launch_spmv(AT_, EvalATEpi<false>{d}, d.p_e2, d.lp_e2, st_); });
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
 std::vector<double> Solve::trace() const {
   Ctl c;
   PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
@@ -1097,7 +1165,7 @@ std::vector<double> Solve::trace() const {
   return tr;
 }
 
-cupdlpx_result_t *Solve::result(const lp_problem_t *prob) {
+cupdlpx_result_t *Solve::result() {
   Dev &d = d_;
   const int n = d.n, m = d.m;
   launch_spmv(AT_, ReducedCostEpi{d}, nullptr, nullptr, st_);
@@ -1124,12 +1192,12 @@ cupdlpx_result_t *Solve::result(const lp_problem_t *prob) {
   Ctl c;
   PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
-  r->num_variables = prob->num_variables;
-  r->num_constraints = prob->num_constraints;
-  r->num_nonzeros = prob->constraint_matrix_num_nonzeros;
-  r->num_reduced_variables = prob->num_variables;
-  r->num_reduced_constraints = prob->num_constraints;
-  r->num_reduced_nonzeros = prob->constraint_matrix_num_nonzeros;
+  r->num_variables = n;
+  r->num_constraints = m;
+  r->num_nonzeros = P_.nnz;
+  r->num_reduced_variables = n;
+  r->num_reduced_constraints = m;
+  r->num_reduced_nonzeros = P_.nnz;
   r->total_count = c.final_t;
   r->rescaling_time_sec = rescale_sec_;
   r->cumulative_time_sec = c.cum_time;

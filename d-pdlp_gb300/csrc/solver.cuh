@@ -2,6 +2,7 @@
 #pragma once
 
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -79,19 +80,43 @@ inline IterFlags iteration_flags(int t, int F) {
   return f;
 }
 
+// An LP resident in HBM, as the caller gave it (unscaled): A and its
+// transpose in CSR with their SpMV plans, bounds, objective, warm start.
+// Read-only once built; any number of solves can run from it.
+struct DevProblem {
+  int m = 0, n = 0, nnz = 0, tile = 0;
+  DevCsr A, AT;  // original values; plan scratch (lcnt/lsum) is per solve
+  double *c = nullptr, *lv = nullptr, *uv = nullptr, *lc = nullptr, *uc = nullptr;
+  double *xs = nullptr, *ys = nullptr;  // warm start (unscaled) or null
+  double cnorm_l2 = 0, cnorm_linf = 0, bnorm_l2 = 0, bnorm_linf = 0, c0 = 0;
+  void *arena = nullptr;
+  size_t bytes = 0;
+  ~DevProblem();
+};
+
+// Validate, transpose (host), plan and upload.  Throws on a malformed CSR.
+DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st);
+
 // One single-LP FP64 solve on one stream.
 class Solve {
  public:
-  Solve(const pdhg_parameters_t &params, cudaStream_t stream, int trace_cap = 0);
+  Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
+        int trace_cap = 0);
   ~Solve();
-  // Upload + transpose + plans + rescale + norms + warm start.
-  void load(const lp_problem_t *prob);
+  // Working copy of the problem, GPU rescaling, finite bounds, warm start.
+  void prepare();
   // Power method -> step size; initial primal weight.
   void init_step();
   // Main loop until termination or iteration limit.
   void run();
   // Reduced cost, unscale, copy to a malloc'ed result.
-  cupdlpx_result_t *result(const lp_problem_t *prob);
+  cupdlpx_result_t *result();
+
+  // Average device time (ms) of the plain-iteration kernels, measured with
+  // CUDA events on the solve's stream over `reps` launches each:
+  // ms[0] primal step (A^T SpMV + update), ms[1] dual step (A SpMV + update),
+  // ms[2] evaluation over A, ms[3] evaluation over A^T.
+  void time_kernels(int reps, double *ms);
 
   // diagnostics
   int power_iterations() const { return pm_iters_; }
@@ -106,7 +131,7 @@ class Solve {
   const DevCsr &AT() const { return AT_; }
 
  private:
-  void alloc(const lp_problem_t *prob);
+  void alloc();
   void enqueue_iteration(int t, int off, bool capture);
   void enqueue_eval(int t, int off, bool infeas, bool restart_check, bool final_eval);
   cudaGraphExec_t chunk_graph(int t0, int t1);
@@ -114,6 +139,7 @@ class Solve {
 
   pdhg_parameters_t p_;
   cudaStream_t st_;
+  const DevProblem &P_;
   Dev d_{};
   DevCsr A_, AT_;
   void *arena_ = nullptr;

@@ -172,6 +172,7 @@ class SolveInfo(C.Structure):
         ("total_seconds", C.c_double),
         ("graphs", C.c_int),
         ("kernel_launches", C.c_longlong),
+        ("device_seconds", C.c_double),
     ]
 
 
@@ -215,6 +216,18 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_gpu_spmv.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_int]
     lib.pdlp_gpu_power_method.restype = C.c_int
     lib.pdlp_gpu_power_method.argtypes = [P, C.POINTER(PdhgParameters), _dp, _ip]
+    lib.pdlp_device_problem_create.restype = C.c_void_p
+    lib.pdlp_device_problem_create.argtypes = [P]
+    lib.pdlp_device_problem_free.restype = None
+    lib.pdlp_device_problem_free.argtypes = [C.c_void_p]
+    lib.pdlp_device_problem_bytes.restype = C.c_longlong
+    lib.pdlp_device_problem_bytes.argtypes = [C.c_void_p]
+    lib.pdlp_device_problem_solve.restype = R
+    lib.pdlp_device_problem_solve.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
+                                              C.POINTER(SolveInfo)]
+    lib.pdlp_device_problem_time_kernels.restype = C.c_int
+    lib.pdlp_device_problem_time_kernels.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
+                                                     C.c_int, _dp]
 
 
 _LIB: C.CDLL | None = None
@@ -372,3 +385,48 @@ def solve(problem: Problem, params: PdhgParameters | None = None, trace_cap: int
         L.cupdlpx_result_free(r)
     inf = {f: getattr(info, f) for f, _ in SolveInfo._fields_}
     return SolveOutput(res, tr[: tl.value].copy(), inf)
+
+
+class DeviceProblem:
+    """An LP resident in HBM (pdlp_device_problem_t)."""
+
+    def __init__(self, problem: Problem, library: C.CDLL | None = None):
+        self._lib = library or lib()
+        self.handle = self._lib.pdlp_device_problem_create(problem.ptr)
+        if not self.handle:
+            raise RuntimeError("upload failed: " + self._lib.pdlp_last_error().decode())
+
+    @property
+    def nbytes(self) -> int:
+        return self._lib.pdlp_device_problem_bytes(self.handle)
+
+    def solve(self, params: PdhgParameters | None = None) -> SolveOutput:
+        info = SolveInfo()
+        pp = C.byref(params) if params is not None else None
+        r = self._lib.pdlp_device_problem_solve(self.handle, pp, C.byref(info))
+        if not r:
+            raise RuntimeError("solve failed: " + self._lib.pdlp_last_error().decode())
+        try:
+            res = result_dict(r)
+        finally:
+            self._lib.cupdlpx_result_free(r)
+        return SolveOutput(res, np.zeros((0, TRACE_WIDTH)),
+                           {f: getattr(info, f) for f, _ in SolveInfo._fields_})
+
+    def time_kernels(self, params: PdhgParameters | None = None, reps: int = 20) -> np.ndarray:
+        ms = np.zeros(4)
+        pp = C.byref(params) if params is not None else None
+        if self._lib.pdlp_device_problem_time_kernels(self.handle, pp, reps, as_dp(ms)) != 0:
+            raise RuntimeError("kernel timing failed: " + self._lib.pdlp_last_error().decode())
+        return ms
+
+    def free(self):
+        if self.handle:
+            self._lib.pdlp_device_problem_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

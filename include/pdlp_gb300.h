@@ -27,6 +27,8 @@ typedef struct {
   double total_seconds;       /* whole solve_lp_problem call */
   int graphs;                 /* distinct iteration-chunk CUDA graphs */
   long long kernel_launches;  /* kernels launched by the solve */
+  double device_seconds;      /* CUDA events on the solve's stream, from the
+                                 first copy/kernel to the result on the host */
 } pdlp_solve_info_t;
 
 /* Number of doubles per trace record written by pdlp_solve_ex: iteration,
@@ -40,6 +42,31 @@ cupdlpx_result_t *pdlp_solve_ex(const lp_problem_t *prob,
                                 const pdhg_parameters_t *params, double *trace,
                                 int trace_cap, int *trace_len,
                                 pdlp_solve_info_t *info);
+
+/* ---- problems resident in HBM ----------------------------------------
+ * An uploaded problem keeps A, its transpose (CSR), the SpMV plans, bounds
+ * and objective on the current device, unscaled, so that any number of
+ * solves can start from HBM without a host copy.  Solves from one handle
+ * may run one after another or concurrently from different threads. */
+typedef struct pdlp_device_problem pdlp_device_problem_t;
+
+pdlp_device_problem_t *pdlp_device_problem_create(const lp_problem_t *prob);
+void pdlp_device_problem_free(pdlp_device_problem_t *dp);
+/* Bytes of HBM the handle holds. */
+long long pdlp_device_problem_bytes(const pdlp_device_problem_t *dp);
+/* Solve from the resident problem (result copied to host, as from
+ * solve_lp_problem). */
+cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
+                                            const pdhg_parameters_t *params,
+                                            pdlp_solve_info_t *info);
+/* Average device milliseconds per launch of the iteration kernels, timed
+ * with CUDA events on the solve's stream over `reps` launches each:
+ * ms[0] primal step (A^T SpMV + projection + Halpern), ms[1] dual step
+ * (A SpMV + projection + Halpern), ms[2] evaluation over A, ms[3]
+ * evaluation over A^T. */
+int pdlp_device_problem_time_kernels(pdlp_device_problem_t *dp,
+                                     const pdhg_parameters_t *params, int reps,
+                                     double *ms);
 
 /* Message of the last failure in this thread ("" if none). */
 const char *pdlp_last_error(void);

@@ -593,12 +593,17 @@ struct Solver {
     ++*len;
   }
 
-  // reference src/solver.cu:54-109
-  void run(double *tr, int cap, int *len) {
+  bool do_restart = false;
+
+  // reference src/solver.cu:54-109; stops early after `budget` iterations
+  // (budget < 0: no budget) so a session can run bounded samples.
+  void run(double *tr, int cap, int *len, long budget = -1) {
     int F = prm.termination_evaluation_frequency;
     auto t0 = std::chrono::steady_clock::now();
-    bool do_restart = false;
+    long done_here = 0;
     while (total < prm.termination_criteria.iteration_limit) {
+      if (budget >= 0 && done_here >= budget) return;
+      ++done_here;
       if (is_major || total == 0 || total % print_frequency(total) == 0) {
         compute_residual();
         if (is_major && total < 3 * F) compute_infeasibility();
@@ -899,6 +904,57 @@ int oracle_coo_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v,
   }
   *nnz_out = nnz;
   return 0;
+}
+
+struct oracle_session {
+  pdhg_parameters_t prm;
+  Solver *s;
+  int nthreads;
+};
+
+oracle_session_t *oracle_session_create(const lp_problem_t *prob,
+                                        const pdhg_parameters_t *params, int nthreads,
+                                        double *setup_sec) {
+  auto *ss = new oracle_session;
+  if (params) ss->prm = *params;
+  else oracle_default_parameters(&ss->prm);
+  ss->nthreads = nthreads;
+  ThreadScope ts(nthreads);
+  auto t0 = std::chrono::steady_clock::now();
+  ss->s = new Solver(ss->prm);
+  ss->s->init(prob);
+  if (setup_sec)
+    *setup_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  // step size from a short power run so the loop can proceed
+  ss->s->eta = 1.0;
+  ss->s->omega = 1.0;
+  ss->s->best_omega = 1.0;
+  return ss;
+}
+
+double oracle_session_power(oracle_session_t *ss, int iters) {
+  ThreadScope ts(ss->nthreads);
+  Solver &s = *ss->s;
+  vec v0;
+  power_start(s.m, v0);
+  auto t0 = std::chrono::steady_clock::now();
+  double smax = power_method(s.A, s.AT, v0, iters, 0.0, nullptr);
+  double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (smax > 0) s.eta = 0.998 / smax;
+  return sec;
+}
+
+double oracle_session_iterate(oracle_session_t *ss, int iters) {
+  ThreadScope ts(ss->nthreads);
+  auto t0 = std::chrono::steady_clock::now();
+  ss->s->run(nullptr, 0, nullptr, iters);
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void oracle_session_free(oracle_session_t *ss) {
+  if (!ss) return;
+  delete ss->s;
+  delete ss;
 }
 
 }  // extern "C"

@@ -81,6 +81,20 @@ int oracle_csc_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v,
 int oracle_coo_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v,
                       int *nnz);
 
+/* Bounded samples for the CPU baseline: a session holds one prepared solve.
+ * create: rescale + transpose + norms (timed, seconds in *setup_sec);
+ * power: `iters` power-method iterations from the reference start vector,
+ *        returns seconds;
+ * iterate: `iters` iterations of the driver loop (evaluations, restarts and
+ *        all) continuing from the current state, returns seconds. */
+typedef struct oracle_session oracle_session_t;
+oracle_session_t *oracle_session_create(const lp_problem_t *prob,
+                                        const pdhg_parameters_t *params,
+                                        int nthreads, double *setup_sec);
+double oracle_session_power(oracle_session_t *s, int iters);
+double oracle_session_iterate(oracle_session_t *s, int iters);
+void oracle_session_free(oracle_session_t *s);
+
 /* Evaluation cadence (reference src/utils.cu:492-501). */
 int oracle_print_frequency(int iter);
 
