@@ -55,6 +55,7 @@ struct Ctl {
   double step_size;       // eta
   double primal_weight;   // omega
   double best_primal_weight;
+  double tau, sigma, inv_sigma;  // eta/omega, eta*omega, 1/sigma
   double best_gap;        // best |log10(rel_d/rel_p)|
   double pw_error_sum;
   double pw_last_error;

@@ -11,11 +11,14 @@ namespace pdlp {
 // y[r] = sum_k a_rk x_k
 struct PlainEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 0;
   static constexpr unsigned MAXMASK = 0;
   const double *x;
   double *y;
   __device__ bool init() { return true; }
+  __device__ void prologue(double *) const {}
+  __device__ void bind(const double *) {}
   __device__ double gather(int j) const { return x[j]; }
   __device__ void row(int r, double s, double *) const { y[r] = s; }
 };

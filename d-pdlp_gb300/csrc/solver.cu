@@ -25,24 +25,41 @@
 namespace pdlp {
 
 // ======================================================= SpMV epilogues
+// Epilogues without per-block scalars.
+#define PDLP_NO_BLOCK_SCALARS                        \
+  __device__ void prologue(double *) const {}        \
+  __device__ void bind(const double *) {}
+
+// Halpern weight w = (k+1)/(k+2), k = inner iteration count
+// (reference pdlp_core_op.cu:559-567), formed once per block.
+__device__ __forceinline__ void halpern_weight(const Ctl *c, int off, double *sc) {
+  int k = c->t_base + off - c->restart_t;
+  double w = (double)(k + 1) / (double)(k + 2);
+  sc[0] = w;
+  sc[1] = 1.0 - w;
+}
+
 template <bool MAJOR, bool FPE>
 struct PrimalEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = FPE ? 1 : 0;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
   int off;
   const double *xcur, *ycur;
   double *xnext;
-  double tau, w;
+  double tau, w, omw;
   __device__ bool init() {
     const Ctl *c = d.ctl;
     if (c->done) return false;
-    int t = c->t_base + off;
-    int k = t - c->restart_t;
-    w = (double)(k + 1) / (double)(k + 2);
-    tau = c->step_size / c->primal_weight;
+    tau = c->tau;
     return true;
+  }
+  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
+  __device__ void bind(const double *sc) {
+    w = sc[0];
+    omw = sc[1];
   }
   __device__ double gather(int i) const { return ycur[i]; }
   __device__ void row(int j, double s, double *acc) const {
@@ -60,34 +77,40 @@ struct PrimalEpi {
       d.dx[j] = dd;
       acc[0] += dd * dd;
     }
-    double refl = d.rho * xr + (1.0 - d.rho) * xc;
-    xnext[j] = w * refl + (1.0 - w) * d.x0[j];
+    double refl = d.rho_is_one ? xr : d.rho * xr + d.one_minus_rho * xc;
+    xnext[j] = w * refl + omw * d.x0[j];
   }
 };
 
 template <bool MAJOR, bool FPE>
 struct DualEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = FPE ? 1 : 0;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
   int off;
   const double *ycur;
   double *ynext;
-  double sigma, w;
+  double sigma, inv_sigma, w, omw;
   __device__ bool init() {
     const Ctl *c = d.ctl;
     if (c->done) return false;
-    int t = c->t_base + off;
-    int k = t - c->restart_t;
-    w = (double)(k + 1) / (double)(k + 2);
-    sigma = c->step_size * c->primal_weight;
+    sigma = c->sigma;
+    inv_sigma = c->inv_sigma;
     return true;
+  }
+  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
+  __device__ void bind(const double *sc) {
+    w = sc[0];
+    omw = sc[1];
   }
   __device__ double gather(int j) const { return d.xref[j]; }
   __device__ void row(int i, double s, double *acc) const {
     double yc = ycur[i];
-    double t = yc / sigma - s;
+    // the reference divides by sigma; one reciprocal per launch instead
+    // (at most 1 ulp apart; an FP64 division costs ~10 FP64 issue slots)
+    double t = yc * inv_sigma - s;
     double tp = fmax(-d.uc[i], fmin(t, -d.lc[i]));
     double yh = (t - tp) * sigma;
     if (MAJOR) d.yhat[i] = yh;
@@ -97,8 +120,8 @@ struct DualEpi {
       d.dy[i] = dd;
       acc[0] += dd * dd;
     }
-    double refl = d.rho * yr + (1.0 - d.rho) * yc;
-    ynext[i] = w * refl + (1.0 - w) * d.y0[i];
+    double refl = d.rho_is_one ? yr : d.rho * yr + d.one_minus_rho * yc;
+    ynext[i] = w * refl + omw * d.y0[i];
   }
 };
 
@@ -106,9 +129,11 @@ struct DualEpi {
 template <bool RESTART_ONLY>
 struct FpeEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 1;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() {
     if (d.ctl->done) return false;
     if (RESTART_ONLY && !d.ctl->do_restart) return false;
@@ -122,9 +147,11 @@ struct FpeEpi {
 template <bool LINF>
 struct EvalAEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 2;
   static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
   Dev d;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return !d.ctl->done; }
   __device__ double gather(int j) const { return d.xhat[j]; }
   __device__ void row(int i, double s, double *acc) const {
@@ -140,9 +167,11 @@ struct EvalAEpi {
 template <bool LINF>
 struct EvalATEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 3;
   static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
   Dev d;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return !d.ctl->done; }
   __device__ double gather(int i) const { return d.yhat[i]; }
   __device__ void row(int j, double s, double *acc) const {
@@ -163,11 +192,13 @@ __device__ __forceinline__ double ray_scale(const Ctl *c) {
 // primal ray over A (utils.cu:561-572, :588-600)
 struct InfAEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 2;
   static constexpr unsigned MAXMASK = 1u;
   Dev d;
   double sc;
-  __device__ bool init() {
+  PDLP_NO_BLOCK_SCALARS
+  __device__ bool init() {  // runs twice per solve: a per-thread division is fine
     if (d.ctl->done) return false;
     sc = ray_scale(d.ctl);
     return true;
@@ -186,10 +217,12 @@ struct InfAEpi {
 // as in the reference call at utils.cu:772-776)
 struct InfATEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 3;
   static constexpr unsigned MAXMASK = 2u;
   Dev d;
   double sc;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() {
     if (d.ctl->done) return false;
     sc = ray_scale(d.ctl);
@@ -209,9 +242,11 @@ struct InfATEpi {
 // reduced cost (pdlp_core_op.cu:31-40)
 struct ReducedCostEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 0;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return true; }
   __device__ double gather(int i) const { return d.yhat[i]; }
   __device__ void row(int j, double s, double *) const {
@@ -222,11 +257,13 @@ struct ReducedCostEpi {
 // power method: g = A^T (inv * v)   (utils.cu:127-136)
 struct PowAtEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 0;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
   const double *v;
   double inv;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() {
     if (d.ctl->pm_done) return false;
     inv = d.ctl->pm_inv_norm;
@@ -239,12 +276,14 @@ struct PowAtEpi {
 // power method: v' = A g, sum q.v', sum v'^2   (utils.cu:138-144)
 struct PowAEpi {
   using val_t = double;
+  using acc_t = double;
   static constexpr int NF = 2;
   static constexpr unsigned MAXMASK = 0;
   Dev d;
   const double *v;
   double *vnext;
   double inv;
+  PDLP_NO_BLOCK_SCALARS
   __device__ bool init() {
     if (d.ctl->pm_done) return false;
     inv = d.ctl->pm_inv_norm;
@@ -258,6 +297,14 @@ struct PowAEpi {
     acc[1] += s * s;
   }
 };
+
+// step sizes derived from eta and omega (reference pdlp_core_op.cu:512, :545)
+__device__ __forceinline__ void set_steps(Ctl *c) {
+  c->tau = c->step_size / c->primal_weight;
+  c->sigma = c->step_size * c->primal_weight;
+  c->inv_sigma = 1.0 / c->sigma;
+}
+__global__ void k_set_steps(Ctl *c) { set_steps(c); }
 
 // ================================================================ launch
 template <class Epi>
@@ -371,6 +418,7 @@ __global__ void __launch_bounds__(kThreads) k_restart_fin(Dev d, int off) {
     c->best_gap = g;
     c->best_primal_weight = c->primal_weight;
   }
+  set_steps(c);
   c->restart_t = c->t_base + off;
   c->last_trial_fixed_point_error = INFINITY;
 }
@@ -880,6 +928,8 @@ void Solve::prepare() {
   auto t0 = std::chrono::steady_clock::now();
   d.c0 = P_.c0;
   d.rho = p_.reflection_coefficient;
+  d.one_minus_rho = 1.0 - d.rho;
+  d.rho_is_one = d.rho == 1.0;
   d.F = p_.termination_evaluation_frequency > 0 ? p_.termination_evaluation_frequency : 1;
   d.linf = p_.optimality_norm == NORM_TYPE_L_INF;
   d.cnorm = d.linf ? P_.cnorm_linf : P_.cnorm_l2;
@@ -1002,6 +1052,8 @@ void Solve::init_step() {
   // ctl offsets of step_size/primal_weight/best_primal_weight are the first 3 doubles
   double s[3] = {eta, omega, omega};
   PDLP_CUDA(cudaMemcpyAsync(d.ctl, s, sizeof(s), cudaMemcpyHostToDevice, st_));
+  k_set_steps<<<1, 1, 0, st_>>>(d.ctl);
+  PDLP_LAUNCH_CHECK();
   PDLP_CUDA(cudaStreamSynchronize(st_));
 }
 
@@ -1043,9 +1095,9 @@ void Solve::enqueue_iteration(int t, int off, bool) {
   }
 #define PDLP_STEPS(MAJ, FP)                                                         \
   {                                                                                 \
-    PrimalEpi<MAJ, FP> pe{d, off, xc, yc, xn, 0.0, 0.0};                            \
+    PrimalEpi<MAJ, FP> pe{d, off, xc, yc, xn, 0.0, 0.0, 0.0};                       \
     launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                               \
-    DualEpi<MAJ, FP> de{d, off, yc, yn, 0.0, 0.0};                                  \
+    DualEpi<MAJ, FP> de{d, off, yc, yn, 0.0, 0.0, 0.0, 0.0};                        \
     launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                                \
   }
   if (f.major_kernel) {
@@ -1146,8 +1198,8 @@ void Solve::time_kernels(int reps, double *ms) {
     PDLP_CUDA(cudaEventElapsedTime(&t, e0, e1));
     return (double)t / reps;
   };
-  PrimalEpi<false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], 0.0, 0.0};
-  DualEpi<false, false> de{d, 0, d.y[0], d.y[1], 0.0, 0.0};
+  PrimalEpi<false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], 0.0, 0.0, 0.0};
+  DualEpi<false, false> de{d, 0, d.y[0], d.y[1], 0.0, 0.0, 0.0, 0.0};
   ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
   ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
   ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<false>{d}, d.p_e1, d.lp_e1, st_); });

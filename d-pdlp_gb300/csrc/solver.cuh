@@ -36,7 +36,8 @@ struct Dev {
   double *trace;
   int trace_cap;
   // constants
-  double cb, ob, c0, cnorm, bnorm, rho;
+  double cb, ob, c0, cnorm, bnorm, rho, one_minus_rho;
+  int rho_is_one;
   int F, linf, verbose;
   double eps_opt, eps_feas, eps_inf, time_limit;
   double art, suff, nec, kp, ki, kd, ismooth;

@@ -10,10 +10,13 @@
 // cuts the rows into thread-block tiles of at most TILE non-zeros:
 //   * light tile : consecutive rows [r0, r1) whose non-zeros fit in TILE; the
 //                  block streams the tile's values and column indices with
-//                  coalesced loads, gathers x, stages the products in shared
-//                  memory and reduces each row with a group of G lanes
-//                  (G = 256 / rows, power of two, at most 32; one whole block
-//                  when the tile holds a single row);
+//                  coalesced loads, gathers x and stages (value, x) pairs in
+//                  shared memory.  Short rows (at most 64 non-zeros on
+//                  average): each lane folds 8 consecutive pairs, then each
+//                  row adds its 1-3 segment partials -- every FP64 instruction
+//                  runs with all 32 lanes.  Few long rows: a group of G lanes
+//                  per row (G = 256 / rows, power of two, at most 32); a tile
+//                  with one row uses the whole block;
 //   * long row   : a row with more than TILE non-zeros is cut into chunks, one
 //                  block each; the last block to finish (atomic ticket) sums
 //                  the chunk partials in chunk order and runs the epilogue.
@@ -99,88 +102,158 @@ __device__ __forceinline__ void block_reduce_fields(double (&acc)[NF > 0 ? NF : 
 }
 
 // Epi must provide:
-//   using val_t; static constexpr int NF; static constexpr unsigned MAXMASK;
-//   __device__ bool init();                       // false: skip (uniform)
-//   __device__ double gather(int col) const;      // x[col] (any transform)
-//   __device__ void row(int r, double sum, double *acc) const;
+//   using val_t;  (matrix value and gathered vector type)
+//   using acc_t;  (accumulation type of the row sums)
+//   static constexpr int NF; static constexpr unsigned MAXMASK;
+//   __device__ bool init();                   // all threads; false: skip (uniform)
+//   __device__ void prologue(double *sc);     // thread 0: per-block scalars
+//   __device__ void bind(const double *sc);   // all threads, after the barrier
+//   __device__ val_t gather(int col) const;   // x[col] (any transform)
+//   __device__ void row(int r, acc_t sum, double *acc) const;
+//
+// GB300 executes FP64 at about 2 lanes per clock per SM, so an FP64 sweep is
+// bound by FP64 issue as much as by HBM.  The kernel therefore spends exactly
+// one fused multiply-add per non-zero: phase 1 stages (value, x[col]) pairs
+// in shared memory with coalesced loads, phase 2 folds each row with FMA, and
+// scalars that need a division (step sizes, Halpern weight) are formed once
+// per block by thread 0.
+// Shared-memory swizzle for the staged (value, x) pairs: phase 1 writes
+// consecutive elements per lane, the stream phase reads 8 consecutive elements
+// per lane (lane stride 8); XOR-ing the low 3 bits with higher index bits makes
+// both patterns bank-conflict free for 4- and 8-byte elements.
+template <class T>
+__device__ __forceinline__ int swz(int i) {
+  return i ^ ((i >> (sizeof(T) == 8 ? 4 : 5)) & 7);
+}
+
 template <int TILE, class Epi>
 __global__ void __launch_bounds__(kThreads)
     spmv_fused(const int *__restrict__ ptr, const int *__restrict__ col,
                const typename Epi::val_t *__restrict__ val, SpmvPlan plan,
                double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
+  using T = typename Epi::val_t;
+  using A = typename Epi::acc_t;
   constexpr int NF = Epi::NF;
   constexpr int IPT = TILE / kThreads;
-  __shared__ double prod[TILE];
+  constexpr int SEG = 8;  // elements per lane in the stream phase
+  __shared__ T sv[TILE];  // values; reused for stream-phase segment partials
+  __shared__ T sx[TILE];  // gathered x
+  __shared__ int soff[kMaxRowsPerTile + 1];
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
+  __shared__ double sc[4];
   __shared__ int s_last;
 
   if (!epi.init()) return;
+  if (threadIdx.x == 0) epi.prologue(sc);
   const int4 b = plan.blk[blockIdx.x];
   const int k0 = b.z, len = b.w - b.z;
+  const int R = b.y >= 0 ? b.y - b.x : 0;
   double acc[NF > 0 ? NF : 1];
 #pragma unroll
   for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
 
-  // Phase 1: coalesced stream of values / columns, gather of x.
+  // Phase 1: coalesced stream of values / columns, gather of x, row offsets.
   {
     int cidx[IPT];
-    double v[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
       int i = threadIdx.x + u * kThreads;
       if (i < len) {
         cidx[u] = ld_stream(col + k0 + i);
-        v[u] = (double)ld_stream(val + k0 + i);
+        sv[swz<T>(i)] = ld_stream(val + k0 + i);
       }
     }
+    for (int j = threadIdx.x; j <= R; j += kThreads) soff[j] = ptr[b.x + j] - k0;
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
       int i = threadIdx.x + u * kThreads;
-      if (i < len) prod[i] = v[u] * epi.gather(cidx[u]);
+      if (i < len) sx[swz<T>(i)] = epi.gather(cidx[u]);
     }
   }
   __syncthreads();
+  epi.bind(sc);
 
-  if (b.y >= 0) {
-    const int r0 = b.x, R = b.y - b.x;
+  if (b.y >= 0 && R > 1 && len <= 64 * R) {
+    // Stream phase: lane t folds elements [8t, 8t+8) with FMA, all lanes busy;
+    // each finished segment's partial goes to sv[swz(start)], a slot the lane
+    // has already consumed.
+    const int beg = threadIdx.x * SEG;
+    if (beg < len) {
+      const int end = beg + SEG < len ? beg + SEG : len;
+      int lo = 0, hi = R;  // row j with soff[j] <= beg < soff[j+1]
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (soff[mid] <= beg) lo = mid;
+        else hi = mid;
+      }
+      int j = lo, nb = soff[j + 1], segs = beg;
+      A s = A(0);
+      for (int e = beg; e < end; ++e) {
+        while (e == nb) {
+          if (segs < e) sv[swz<T>(segs)] = (T)s;
+          s = A(0);
+          segs = e;
+          ++j;
+          nb = soff[j + 1];
+        }
+        s = fma((A)sv[swz<T>(e)], (A)sx[swz<T>(e)], s);
+      }
+      sv[swz<T>(segs)] = (T)s;
+    }
+    __syncthreads();
+    // Row fold: segment at the row start, then one per lane boundary inside.
+    for (int j = threadIdx.x; j < R; j += kThreads) {
+      const int a = soff[j], e = soff[j + 1];
+      A sum = A(0);
+      if (a < e) {
+        sum = (A)sv[swz<T>(a)];
+        for (int q = (a / SEG + 1) * SEG; q < e; q += SEG) sum += (A)sv[swz<T>(q)];
+      }
+      epi.row(b.x + j, sum, acc);
+    }
+  } else if (b.y >= 0) {
+    const int r0 = b.x;
     if (R == 1) {
-      double s = 0.0;
-      for (int i = threadIdx.x; i < len; i += kThreads) s += prod[i];
-      double t[1] = {s};
-      block_sum<1>(t, red);
-      if (threadIdx.x == 0) epi.row(r0, t[0], acc);
-    } else {
-      int g = kThreads / (R > 0 ? R : 1);
+      A s = A(0);
+      for (int i = threadIdx.x; i < len; i += kThreads)
+        s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
+      A v = warp_sum(s);
+      int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (lane == 0) red[wid] = (double)v;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        A tot = A(0);
+        for (int w = 0; w < kThreads / 32; ++w) tot += (A)red[w];
+        epi.row(r0, tot, acc);
+      }
+    } else if (R > 1) {
+      // few long rows: a group of G lanes per row
+      int g = kThreads / R;
       int G = 1;
       while (G * 2 <= g && G < 32) G *= 2;
-      if (G == 1) {
-        for (int r = r0 + threadIdx.x; r < b.y; r += kThreads) {
-          int beg = ptr[r] - k0, end = ptr[r + 1] - k0;
-          double s = 0.0;
-          for (int i = beg; i < end; ++i) s += prod[i];
-          epi.row(r, s, acc);
-        }
-      } else {
-        int grp = threadIdx.x / G, li = threadIdx.x & (G - 1);
-        int r = r0 + grp;
-        double s = 0.0;
-        if (grp < R) {
-          int beg = ptr[r] - k0, end = ptr[r + 1] - k0;
-          for (int i = beg + li; i < end; i += G) s += prod[i];
-        }
-        for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (li == 0 && grp < R) epi.row(r, s, acc);
+      int grp = threadIdx.x / G, li = threadIdx.x & (G - 1);
+      A s = A(0);
+      if (grp < R) {
+        int beg = soff[grp], end = soff[grp + 1];
+        for (int i = beg + li; i < end; i += G) s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
       }
+      for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (li == 0 && grp < R) epi.row(r0 + grp, s, acc);
     }
   } else {
     // chunk of a long row
-    double s = 0.0;
-    for (int i = threadIdx.x; i < len; i += kThreads) s += prod[i];
-    double t[1] = {s};
-    block_sum<1>(t, red);
+    A s = A(0);
+    for (int i = threadIdx.x; i < len; i += kThreads)
+      s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
+    A v = warp_sum(s);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = (double)v;
+    __syncthreads();
     const int lid = -b.y - 1;
     if (threadIdx.x == 0) {
-      plan.lsum[blockIdx.x] = t[0];
+      A tot = A(0);
+      for (int w = 0; w < kThreads / 32; ++w) tot += (A)red[w];
+      plan.lsum[blockIdx.x] = (double)tot;
       __threadfence();
       unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
       s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
@@ -189,8 +262,8 @@ __global__ void __launch_bounds__(kThreads)
     if (s_last && threadIdx.x == 0) {
       __threadfence();
       const int2 L = plan.lrow[lid];
-      double tot = 0.0;
-      for (int c = 0; c < L.y; ++c) tot += __ldcg(plan.lsum + L.x + c);
+      A tot = A(0);
+      for (int c = 0; c < L.y; ++c) tot += (A)__ldcg(plan.lsum + L.x + c);
       double lacc[NF > 0 ? NF : 1];
 #pragma unroll
       for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
@@ -204,6 +277,7 @@ __global__ void __launch_bounds__(kThreads)
   }
 
   if constexpr (NF > 0) {
+    __syncthreads();
     block_reduce_fields<NF, Epi::MAXMASK>(acc, red);
     if (threadIdx.x == 0) {
 #pragma unroll
