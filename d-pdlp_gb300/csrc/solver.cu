@@ -314,6 +314,9 @@ void launch_spmv(const DevCsr &M, const Epi &epi, double *part, double *lpart,
   if (M.plan.tile == 2048)
     spmv_fused<2048, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
                                                              part, lpart, epi);
+  else if (M.plan.tile == 1024)
+    spmv_fused<1024, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
+                                                             part, lpart, epi);
   else
     spmv_fused<512, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
                                                             part, lpart, epi);
@@ -701,7 +704,15 @@ void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax
     }
 }
 
-static int pick_tile(long nnz) { return nnz >= 2000000 ? 2048 : 512; }
+// Non-zeros per thread-block tile.  PDLP_SPMV_TILE (512, 1024 or 2048)
+// overrides the size rule.
+static int pick_tile(long nnz) {
+  if (const char *e = getenv("PDLP_SPMV_TILE")) {
+    int t = atoi(e);
+    if (t == 512 || t == 1024 || t == 2048) return t;
+  }
+  return nnz >= 2000000 ? 2048 : 512;
+}
 
 DevProblem::~DevProblem() {
   if (arena) cudaFree(arena);
