@@ -147,11 +147,11 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def kernel_bytes(m, n, nnz):
-    """Algorithmic bytes per launch of the two iteration kernels (FP64 values,
-    int32 indices, each vector touched once)."""
-    primal = 12 * nnz + 4 * (n + 1) + 8 * m + 7 * 8 * n   # A^T stream, gather y, 5 reads + 2 writes of n
-    dual = 12 * nnz + 4 * (m + 1) + 8 * n + 5 * 8 * m     # A stream, gather x_ref, 4 reads + 1 write of m
+def kernel_bytes(m, n, nnz, s=8):
+    """Algorithmic bytes per launch of the two iteration kernels (values and
+    vectors of s bytes, int32 indices, each vector touched once)."""
+    primal = (s + 4) * nnz + 4 * (n + 1) + s * m + 7 * s * n   # A^T stream, gather y, 5 reads + 2 writes of n
+    dual = (s + 4) * nnz + 4 * (m + 1) + s * n + 5 * s * m     # A stream, gather x_ref, 4 reads + 1 write of m
     return primal, dual
 
 
@@ -206,18 +206,20 @@ def run_ours(args, cp, rank, world, local):
     a = prob.arrays()
     m, n, nnz = a["m"], a["n"], a["nnz"]
     params = params_for(cp, args.eps)
+    prec = cp.PRECISION_FP32_REFINE if args.precision == "fp32" else cp.PRECISION_FP64
     dp = cp.DeviceProblem(prob)
     for _ in range(args.warmup):
-        out = dp.solve(params)
+        out = dp.solve(params, precision=prec)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
     dev_s, wall_s, launches, last = [], [], 0, None
+    fp64 = None
     with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0])
                       if world > 1 else 0) as clk:
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            out = dp.solve(params)
+            out = dp.solve(params, precision=prec)
             wall_s.append(time.perf_counter() - t0)
             dev_s.append(out.info["device_seconds"])
             launches += out.info["kernel_launches"]
@@ -226,8 +228,22 @@ def run_ours(args, cp, rank, world, local):
         e2e_s = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            eo = cp.solve(prob, params)
+            eo = cp.solve(prob, params, precision=prec)
             e2e_s.append(time.perf_counter() - t0)
+        if prec != cp.PRECISION_FP64 and args.fp64_steps > 0:
+            # the plain FP64 solve of the same LP, for the FP32-vs-FP64 half of the metric
+            f_dev, f_last = [], None
+            for i in range(args.fp64_steps + 1):
+                fo = dp.solve(params, precision=cp.PRECISION_FP64)
+                if i:
+                    f_dev.append(fo.info["device_seconds"])
+                    f_last = fo
+            fp64 = {"value": round(statistics.mean(f_dev), 4), "unit": "s", "steps": len(f_dev),
+                    "warmup": 1, "iterations": f_last.result["total_count"],
+                    "status": f_last.result["status"],
+                    "primal_obj": f_last.result["primal_objective_value"],
+                    "us_per_iteration": round(f_last.info["loop_seconds"] /
+                                              max(1, f_last.result["total_count"]) * 1e6, 2)}
     clocks = clk.summary()
     value = statistics.mean(dev_s)
     if world > 1:
@@ -239,8 +255,8 @@ def run_ours(args, cp, rank, world, local):
     else:
         e2e_mean = statistics.mean(e2e_s)
     r = last.result
-    ms = dp.time_kernels(params, reps=args.kernel_reps)
-    pb, db = kernel_bytes(m, n, nnz)
+    ms = dp.time_kernels(params, reps=args.kernel_reps, precision=prec)
+    pb, db = kernel_bytes(m, n, nnz, 4 if prec != cp.PRECISION_FP64 else 8)
     kernels = {"primal_step": (ms[0], pb), "dual_step": (ms[1], db)}
     dom = max(kernels, key=lambda k: kernels[k][0])
     peak, peak_kind = load_peaks()
@@ -252,10 +268,14 @@ def run_ours(args, cp, rank, world, local):
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1e3, 2),
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 iterates + f64 KKT/refinement" if prec != cp.PRECISION_FP64 else "f64",
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": name, "description": WORKLOADS[name]["desc"], "m": m, "n": n,
-                   "nnz": nnz, "precision": "FP64 plain PDHG", "eps": args.eps,
+                   "nnz": nnz, "eps": args.eps,
+                   "precision": ("FP32 PDHG + FP64 iterative refinement (FP64 KKT of the "
+                                 "original LP meets eps)") if prec != cp.PRECISION_FP64
+                   else "FP64 plain PDHG",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs (A and A^T, 480 MB) larger than L2; no flush needed"},
         "e2e": {"value": round(e2e_mean, 4), "unit": "s", "h2d_bytes_per_step": h2d,
@@ -282,8 +302,14 @@ def run_ours(args, cp, rank, world, local):
                   "us_per_iteration": round(last.info["loop_seconds"] / max(iters, 1) * 1e6, 2)},
         "clocks": clocks,
     }
+    if fp64 is not None:
+        line["fp64"] = fp64
+    if prec != cp.PRECISION_FP64:
+        line["solve"]["refinement_rounds"] = last.info["refinement_rounds"]
     if rank == 0 and not args.no_cpu_baseline:
-        cpu_v, desc, parts = cpu_sample(cp, prob, params, iters, pm_iters)
+        # the CPU oracle runs the FP64 algorithm: extrapolate with the FP64 iteration count
+        f_iters = fp64["iterations"] if fp64 is not None else iters
+        cpu_v, desc, parts = cpu_sample(cp, prob, params, f_iters, pm_iters)
         line["cpu_baseline"] = {"value": round(cpu_v, 2), "unit": "s", "cores": os.cpu_count(),
                                 "kind": "port", "sample": desc, "parts": parts}
     dp.free()
@@ -332,6 +358,10 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-4)
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32",
+                    help="fp32: FP32 iterates + FP64 refinement (default); fp64: plain FP64")
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="timed FP64 solves reported beside an FP32 run (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     os.environ.setdefault("PDLP_QUIET", "1")

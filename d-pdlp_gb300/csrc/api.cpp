@@ -237,7 +237,7 @@ cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &
                             cudaStream_t st, double *trace, int trace_cap, int *trace_len,
                             pdlp_solve_info_t *info,
                             std::chrono::steady_clock::time_point t0) {
-  pdlp::Solve s(p, st, P, trace ? trace_cap : 0);
+  pdlp::Solve<double> s(p, st, P, trace ? trace_cap : 0);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (info) {
     PDLP_CUDA(cudaEventCreate(&ev0));
@@ -277,8 +277,51 @@ cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &
     info->total_seconds = std::chrono::duration<double>(t3 - t0).count();
     info->graphs = s.graph_count();
     info->kernel_launches = s.kernel_launches();
+    info->precision = PDLP_PRECISION_FP64;
   }
   return r;
+}
+
+cupdlpx_result_t *run_refined(const pdlp::DevProblem &P, const pdhg_parameters_t &p,
+                              const pdlp_options_t &o, cudaStream_t st,
+                              pdlp_solve_info_t *info,
+                              std::chrono::steady_clock::time_point t0) {
+  pdlp::RefineOptions ro;
+  if (o.max_refinements > 0) ro.max_rounds = o.max_refinements;
+  ro.inner_eps = o.inner_eps;
+  pdlp::RefineReport rep;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  PDLP_CUDA(cudaEventCreate(&ev0));
+  PDLP_CUDA(cudaEventCreate(&ev1));
+  PDLP_CUDA(cudaEventRecord(ev0, st));
+  cupdlpx_result_t *r = pdlp::solve_refined(P, p, ro, st, &rep);
+  PDLP_CUDA(cudaEventRecord(ev1, st));
+  PDLP_CUDA(cudaEventSynchronize(ev1));
+  float ms = 0.f;
+  PDLP_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (info) {
+    info->device_seconds = ms * 1e-3;
+    info->loop_seconds = rep.seconds;
+    info->total_seconds =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    info->kernel_launches = rep.kernel_launches;
+    info->refinement_rounds = rep.rounds;
+    info->power_iterations = rep.power_iterations;
+    info->sigma_max = rep.sigma_max;
+    info->precision = PDLP_PRECISION_FP32_REFINE;
+  }
+  return r;
+}
+
+pdlp_options_t env_options() {
+  pdlp_options_t o;
+  memset(&o, 0, sizeof(o));
+  const char *e = getenv("PDLP_PRECISION");
+  if (e && (strcmp(e, "fp32") == 0 || strcmp(e, "FP32") == 0))
+    o.precision = PDLP_PRECISION_FP32_REFINE;
+  return o;
 }
 
 bool prepare_params(const pdhg_parameters_t *params, pdhg_parameters_t &p) {
@@ -299,7 +342,7 @@ bool prepare_params(const pdhg_parameters_t *params, pdhg_parameters_t &p) {
 
 cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *params,
                              double *trace, int trace_cap, int *trace_len,
-                             pdlp_solve_info_t *info) {
+                             pdlp_solve_info_t *info, const pdlp_options_t *opts) {
   if (!prob) {
     set_error("solve_lp_problem: invalid arguments.");
     return nullptr;
@@ -311,7 +354,11 @@ cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *
     print_initial_info(&p, prob);
     StreamGuard sg;
     std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
-    cupdlpx_result_t *r = run_solve(*P, p, sg.s, trace, trace_cap, trace_len, info, t0);
+    pdlp_options_t o = opts ? *opts : env_options();
+    cupdlpx_result_t *r =
+        o.precision == PDLP_PRECISION_FP32_REFINE
+            ? run_refined(*P, p, o, sg.s, info, t0)
+            : run_solve(*P, p, sg.s, trace, trace_cap, trace_len, info, t0);
     if (!quiet_summary()) final_log(r, &p);
     return r;
   } catch (const std::exception &e) {
@@ -416,7 +463,15 @@ void set_start_values(lp_problem_t *prob, const double *primal, const double *du
 }
 
 cupdlpx_result_t *solve_lp_problem(const lp_problem_t *prob, const pdhg_parameters_t *params) {
-  return solve_impl(prob, params, nullptr, 0, nullptr, nullptr);
+  return solve_impl(prob, params, nullptr, 0, nullptr, nullptr, nullptr);
+}
+
+cupdlpx_result_t *pdlp_solve_opts(const lp_problem_t *prob, const pdhg_parameters_t *params,
+                                  const pdlp_options_t *opts, pdlp_solve_info_t *info) {
+  if (info) memset(info, 0, sizeof(*info));
+  pdlp_options_t o;
+  memset(&o, 0, sizeof(o));
+  return solve_impl(prob, params, nullptr, 0, nullptr, info, opts ? opts : &o);
 }
 
 void set_default_parameters(pdhg_parameters_t *p) {
@@ -484,7 +539,9 @@ cupdlpx_result_t *pdlp_solve_ex(const lp_problem_t *prob, const pdhg_parameters_
                                 pdlp_solve_info_t *info) {
   if (trace_len) *trace_len = 0;
   if (info) memset(info, 0, sizeof(*info));
-  return solve_impl(prob, params, trace, trace_cap, trace_len, info);
+  pdlp_options_t o;
+  memset(&o, 0, sizeof(o));
+  return solve_impl(prob, params, trace, trace_cap, trace_len, info, &o);
 }
 
 const char *pdlp_last_error(void) { return g_last_error.c_str(); }
@@ -498,14 +555,14 @@ int pdlp_gpu_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params, 
   try {
     StreamGuard sg;
     std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
-    pdlp::Solve s(*params, sg.s, *P, 0);
+    pdlp::Solve<double> s(*params, sg.s, *P, 0);
     s.prepare();
-    const pdlp::Dev &d = s.dev();
+    const pdlp::Dev<double> &d = s.dev();
     const int n = d.n, m = d.m, nnz = s.A().nnz;
     auto get = [&](double *dst, const double *src, int cnt) {
       if (cnt > 0) PDLP_CUDA(cudaMemcpy(dst, src, (size_t)cnt * 8, cudaMemcpyDeviceToHost));
     };
-    get(vals, s.A().val, nnz);
+    get(vals, s.A64().val, nnz);
     get(c, d.c, n);
     get(lv, d.lv, n);
     get(uv, d.uv, n);
@@ -528,7 +585,7 @@ int pdlp_gpu_power_method(const lp_problem_t *prob, const pdhg_parameters_t *par
   try {
     StreamGuard sg;
     std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
-    pdlp::Solve s(*params, sg.s, *P, 0);
+    pdlp::Solve<double> s(*params, sg.s, *P, 0);
     s.prepare();
     s.init_step();
     *sigma_max = s.sigma_max();
@@ -566,6 +623,15 @@ long long pdlp_device_problem_bytes(const pdlp_device_problem_t *dp) {
 cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
                                             const pdhg_parameters_t *params,
                                             pdlp_solve_info_t *info) {
+  pdlp_options_t o;
+  memset(&o, 0, sizeof(o));
+  return pdlp_device_problem_solve_opts(dp, params, &o, info);
+}
+
+cupdlpx_result_t *pdlp_device_problem_solve_opts(pdlp_device_problem_t *dp,
+                                                 const pdhg_parameters_t *params,
+                                                 const pdlp_options_t *opts,
+                                                 pdlp_solve_info_t *info) {
   if (!dp || !dp->P) {
     set_error("pdlp_device_problem_solve: NULL handle.");
     return nullptr;
@@ -576,7 +642,12 @@ cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
   auto t0 = std::chrono::steady_clock::now();
   try {
     StreamGuard sg;
-    cupdlpx_result_t *r = run_solve(*dp->P, p, sg.s, nullptr, 0, nullptr, info, t0);
+    pdlp_options_t o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    cupdlpx_result_t *r = o.precision == PDLP_PRECISION_FP32_REFINE
+                              ? run_refined(*dp->P, p, o, sg.s, info, t0)
+                              : run_solve(*dp->P, p, sg.s, nullptr, 0, nullptr, info, t0);
     if (!quiet_summary()) final_log(r, &p);
     return r;
   } catch (const std::exception &e) {
@@ -588,15 +659,28 @@ cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
 
 int pdlp_device_problem_time_kernels(pdlp_device_problem_t *dp, const pdhg_parameters_t *params,
                                      int reps, double *ms) {
+  return pdlp_device_problem_time_kernels_prec(dp, params, PDLP_PRECISION_FP64, reps, ms);
+}
+
+int pdlp_device_problem_time_kernels_prec(pdlp_device_problem_t *dp,
+                                          const pdhg_parameters_t *params, int precision,
+                                          int reps, double *ms) {
   if (!dp || !dp->P || !ms || reps <= 0) return -1;
   pdhg_parameters_t p;
   if (!prepare_params(params, p)) return -1;
   try {
     StreamGuard sg;
-    pdlp::Solve s(p, sg.s, *dp->P, 0);
-    s.prepare();
-    s.init_step();
-    s.time_kernels(reps, ms);
+    if (precision == PDLP_PRECISION_FP32_REFINE) {
+      pdlp::Solve<float> s(p, sg.s, *dp->P, 0);
+      s.prepare();
+      s.init_step();
+      s.time_kernels(reps, ms);
+    } else {
+      pdlp::Solve<double> s(p, sg.s, *dp->P, 0);
+      s.prepare();
+      s.init_step();
+      s.time_kernels(reps, ms);
+    }
     return 0;
   } catch (const std::exception &e) {
     set_error(std::string("pdlp_device_problem_time_kernels: ") + e.what());

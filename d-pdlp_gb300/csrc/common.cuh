@@ -70,6 +70,8 @@ struct Ctl {
   double max_primal_ray_inf, max_dual_ray_inf, primal_ray_obj, dual_ray_obj;
   double ray_primal_inf_norm, ray_dual_inf_norm;  // scratch
   double cum_time;
+  double best_err;  // best max(rel_p, rel_d, rel_gap) seen (stall detection)
+  double snap_err;  // error of the snapshot iterate (refinement rounds)
   // iteration counters
   int t_base;       // iteration number of the first iteration of the chunk
   int restart_t;    // total_count at the last restart (inner = t - restart_t)
@@ -78,7 +80,8 @@ struct Ctl {
   int reason;       // termination_reason_t
   int final_t;      // total_count at termination
   int trace_len;
-  int pad0;
+  int best_err_t;   // iteration of the last 10% improvement of best_err
+  int snap_now;     // 1: the evaluation just made is the best so far
   unsigned long long t_start_ns;  // %globaltimer at loop start
   // power method (reference utils.cu:66-171)
   double pm_inv_norm;

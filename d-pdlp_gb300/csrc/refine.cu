@@ -1,0 +1,348 @@
+// refine.cu -- FP32 PDHG with FP64 iterative refinement.
+//
+// Round 0 solves the LP with FP32 iterates (FP32 SpMVs and updates, FP64
+// reductions).  If the FP64 KKT of the result, evaluated on the original
+// problem, misses the tolerance, each further round re-centres the problem
+// at the FP64 point (xbar, ybar) and solves the correction LP
+//     min (c - A^T ybar)' z
+//     s.t. lc - A xbar <= A z <= uc - A xbar,  lv - xbar <= z <= uv - xbar
+// in FP32, then accumulates xbar += z, ybar += w (w the correction dual) and
+// takes the correction's dual slack as the new one; the correction's KKT
+// residuals are exactly the original residuals of (xbar + z, ybar + w), so
+// its termination test uses the original's bound / objective norms.  FP32
+// only has to represent the correction, which shrinks round after round.
+// Residuals, corrections and the final KKT are FP64 throughout.
+#include <math.h>
+#include <string.h>
+
+#include <chrono>
+
+#include "iter_kernels.cuh"
+
+namespace pdlp {
+
+// over A: s = (A xbar)_i -> shifted constraint bounds
+struct CorrAEpi {
+  using val_t = double;
+  using acc_t = double;
+  static constexpr int NF = 0;
+  static constexpr unsigned MAXMASK = 0;
+  const double *xbar, *lc, *uc;
+  double *lc2, *uc2;
+  PDLP_NO_BLOCK_SCALARS
+  __device__ bool init() { return true; }
+  __device__ double gather(int j) const { return xbar[j]; }
+  __device__ void row(int i, double s, double *) const {
+    lc2[i] = lc[i] - s;
+    uc2[i] = uc[i] - s;
+  }
+};
+
+// over A^T: s = (A^T ybar)_j -> reduced-cost objective, shifted variable bounds
+struct CorrATEpi {
+  using val_t = double;
+  using acc_t = double;
+  static constexpr int NF = 0;
+  static constexpr unsigned MAXMASK = 0;
+  const double *ybar, *c, *lv, *uv, *xbar;
+  double *c2, *lv2, *uv2;
+  PDLP_NO_BLOCK_SCALARS
+  __device__ bool init() { return true; }
+  __device__ double gather(int i) const { return ybar[i]; }
+  __device__ void row(int j, double s, double *) const {
+    c2[j] = c[j] - s;
+    double xb = xbar[j];
+    lv2[j] = lv[j] - xb;
+    uv2[j] = uv[j] - xb;
+  }
+};
+
+// reduced cost rc = c - A^T y of the FP64 point, and the dual slack taken as
+// its projection onto the cone the bounds allow: rc_j where both bounds are
+// finite, max(rc_j, 0) with only a lower bound, min(rc_j, 0) with only an
+// upper bound, 0 for a free variable.  This is the limit of the iteration's
+// (x_hat - t) / tau and, unlike a dual slack carried over from an FP32
+// round, has FP64 accuracy.
+struct RcEpi {
+  using val_t = double;
+  using acc_t = double;
+  static constexpr int NF = 0;
+  static constexpr unsigned MAXMASK = 0;
+  const double *y, *c, *lv, *uv;
+  double *rc, *lam;
+  PDLP_NO_BLOCK_SCALARS
+  __device__ bool init() { return true; }
+  __device__ double gather(int i) const { return y[i]; }
+  __device__ void row(int j, double s, double *) const {
+    double r = c[j] - s;
+    rc[j] = r;
+    bool lo = isfinite(lv[j]), up = isfinite(uv[j]);
+    lam[j] = lo && up ? r : lo ? fmax(r, 0.0) : up ? fmin(r, 0.0) : 0.0;
+  }
+};
+
+__global__ void k_finite(int m, const double *lc, const double *uc, double *lcf, double *ucf) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
+    lcf[i] = isfinite(lc[i]) ? lc[i] : 0.0;
+    ucf[i] = isfinite(uc[i]) ? uc[i] : 0.0;
+  }
+}
+
+// xbar += z, ybar += w, keeping the previous point for a rollback
+__global__ void k_accumulate(int n, int m, double *xbar, double *ybar, double *xold,
+                             double *yold, const double *z, const double *w) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
+    xold[j] = xbar[j];
+    xbar[j] += z[j];
+  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
+    yold[i] = ybar[i];
+    ybar[i] += w[i];
+  }
+}
+
+__global__ void k_rollback(int n, int m, double *xbar, double *ybar, const double *xold,
+                           const double *yold) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) xbar[j] = xold[j];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) ybar[i] = yold[i];
+}
+
+namespace {
+size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+}  // namespace
+
+cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &params,
+                                const RefineOptions &opt, cudaStream_t st,
+                                RefineReport *report) {
+  auto t0 = std::chrono::steady_clock::now();
+  const int n = P.n, m = P.m, nnz = P.nnz;
+  const double eps_feas = params.termination_criteria.eps_feasible_relative;
+  const double eps_opt = params.termination_criteria.eps_optimal_relative;
+  const bool linf = params.optimality_norm == NORM_TYPE_L_INF;
+
+  // device workspace: FP64 point, correction, correction problem vectors,
+  // SpMV scratch for the original matrices
+  size_t bytes = 0;
+  const size_t vn = n, vm = m;
+  auto need = [&](size_t b) { bytes += a256(b + 1); };
+  for (int i = 0; i < 9; ++i) need(vn * 8);  // xbar lam z lz c2 lv2 uv2 rc xold
+  for (int i = 0; i < 7; ++i) need(vm * 8);  // ybar w lc2 uc2 lcf ucf yold
+  need((size_t)P.A.plan.nlong * 4); need((size_t)P.A.plan.nblk * 8);
+  need((size_t)P.AT.plan.nlong * 4); need((size_t)P.AT.plan.nblk * 8);
+  char *mem = nullptr;
+  PDLP_CUDA(cudaMalloc(&mem, bytes));
+  struct Free {
+    char *p;
+    ~Free() { cudaFree(p); }
+  } guard{mem};
+  size_t off = 0;
+  auto take = [&](size_t b) {
+    char *p = mem + off;
+    off += a256(b + 1);
+    return p;
+  };
+  double *xbar = (double *)take(vn * 8), *lam = (double *)take(vn * 8);
+  double *z = (double *)take(vn * 8), *lz = (double *)take(vn * 8);
+  double *c2 = (double *)take(vn * 8), *lv2 = (double *)take(vn * 8);
+  double *uv2 = (double *)take(vn * 8), *rc = (double *)take(vn * 8);
+  double *xold = (double *)take(vn * 8), *yold = (double *)take(vm * 8);
+  double *ybar = (double *)take(vm * 8), *w = (double *)take(vm * 8);
+  double *lc2 = (double *)take(vm * 8), *uc2 = (double *)take(vm * 8);
+  double *olcf = (double *)take(vm * 8), *oucf = (double *)take(vm * 8);
+  if (m) k_finite<<<grid_for(m), kThreads, 0, st>>>(m, P.lc, P.uc, olcf, oucf);
+  DevCsr A = P.A, AT = P.AT;
+  A.plan.lcnt = (unsigned *)take((size_t)P.A.plan.nlong * 4);
+  A.plan.lsum = (double *)take((size_t)P.A.plan.nblk * 8);
+  AT.plan.lcnt = (unsigned *)take((size_t)P.AT.plan.nlong * 4);
+  AT.plan.lsum = (double *)take((size_t)P.AT.plan.nblk * 8);
+  if (P.A.plan.nlong) PDLP_CUDA(cudaMemsetAsync(A.plan.lcnt, 0, (size_t)P.A.plan.nlong * 4, st));
+  if (P.AT.plan.nlong) PDLP_CUDA(cudaMemsetAsync(AT.plan.lcnt, 0, (size_t)P.AT.plan.nlong * 4, st));
+  if (n) {
+    PDLP_CUDA(cudaMemsetAsync(xbar, 0, vn * 8, st));
+    PDLP_CUDA(cudaMemsetAsync(lam, 0, vn * 8, st));
+  }
+  if (m) PDLP_CUDA(cudaMemsetAsync(ybar, 0, vm * 8, st));
+
+  // FP64 evaluator of the original problem (KKT is scaling invariant, so no
+  // rescaling is needed)
+  pdhg_parameters_t pe = params;
+  pe.l_inf_ruiz_iterations = 0;
+  pe.has_pock_chambolle_alpha = false;
+  pe.bound_objective_rescaling = false;
+  Solve<double> ev(pe, st, P, 0);
+  ev.prepare();
+
+  // the correction problem: a view of P's matrices with its own vectors
+  DevProblem Q;
+  Q.m = m;
+  Q.n = n;
+  Q.nnz = nnz;
+  Q.tile = P.tile;
+  Q.A = P.A;
+  Q.AT = P.AT;
+  Q.c = c2;
+  Q.lv = lv2;
+  Q.uv = uv2;
+  Q.lc = lc2;
+  Q.uc = uc2;
+  // original norms: the correction's relative residuals equal the original's
+  Q.cnorm_l2 = P.cnorm_l2;
+  Q.cnorm_linf = P.cnorm_linf;
+  Q.bnorm_l2 = P.bnorm_l2;
+  Q.bnorm_linf = P.bnorm_linf;
+  Q.c0 = 0.0;
+  Q.shift_x = xbar;
+  Q.shift_y = ybar;
+  Q.orig_c = P.c;
+  Q.orig_lcf = olcf;
+  Q.orig_ucf = oucf;
+  Q.orig_c0 = P.c0;
+
+  RefineReport rep;
+  double sigma = 0.0;
+  int reason = TERMINATION_REASON_UNSPECIFIED;
+  long iters = 0, launches = 0;
+  (void)reason;
+  int limit = params.termination_criteria.iteration_limit;
+  Kkt kkt{};
+  double best_err = INFINITY;
+  double omega0 = 1.0, cb0 = 1.0, ob0 = 1.0;
+  reason = TERMINATION_REASON_ITERATION_LIMIT;  // unless a round meets the tolerances
+  cupdlpx_result_t *ray_result = nullptr;
+  double rescale_sec = 0.0;
+  for (int round = 0; round < opt.max_rounds; ++round) {
+    const DevProblem &R = round == 0 ? P : Q;
+    if (round > 0) {
+      launch_spmv(A, CorrAEpi{xbar, P.lc, P.uc, lc2, uc2}, nullptr, nullptr, st);
+      launch_spmv(AT, CorrATEpi{ybar, P.c, P.lv, P.uv, xbar, c2, lv2, uv2}, nullptr, nullptr, st);
+      launches += 2;
+    }
+    pdhg_parameters_t pi = params;
+    pi.termination_criteria.iteration_limit = (int)std::max<long>(0, limit - iters);
+    double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    pi.termination_criteria.time_sec_limit = params.termination_criteria.time_sec_limit - elapsed;
+    if (round > 0) {
+      // a margin below the target, so a round never stops at its first
+      // evaluation on a point the FP64 check just rejected
+      double e = opt.inner_eps > 0.0 ? opt.inner_eps : 0.5;
+      pi.termination_criteria.eps_feasible_relative = opt.inner_eps > 0.0 ? e : e * eps_feas;
+      pi.termination_criteria.eps_optimal_relative = opt.inner_eps > 0.0 ? e : e * eps_opt;
+    }
+    Solve<float> s(pi, st, R, 0);
+    s.prepare();
+    if (round == 0) rescale_sec = s.rescale_seconds();
+    // the primal weight balances scaled primal and dual distances, so it
+    // carries over between rounds in proportion to ob / cb
+    double omega = round == 0 ? 0.0 : omega0 * (s.ob() / s.cb()) / (ob0 / cb0);
+    s.init_step(sigma, omega);
+    if (round == 0) {
+      sigma = s.sigma_max();
+      rep.power_iterations = s.power_iterations();
+      rep.sigma_max = sigma;
+    }
+    s.set_stall_rule(3000, 0.3);  // FP32 has a precision floor: every round must end
+    s.enable_snapshot();
+    s.run();
+    if (round == 0) {
+      omega0 = s.primal_weight();
+      cb0 = s.cb();
+      ob0 = s.ob();
+    }
+    int r = s.reason();
+    iters += s.total_count();
+    launches += s.kernel_launches();
+    rep.rounds = round + 1;
+    if (r == TERMINATION_REASON_PRIMAL_INFEASIBLE || r == TERMINATION_REASON_DUAL_INFEASIBLE) {
+      // infeasibility certificates come from the first round's FP32 rays
+      ray_result = s.result();
+      reason = r;
+      break;
+    }
+    s.result_device(z, w, lz);
+    k_accumulate<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold, z, w);
+    PDLP_LAUNCH_CHECK();
+    launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
+    launches += 2;
+    Kkt k = ev.evaluate(xbar, ybar, lam);
+    launches += 4;
+    double err = fmax(k.rel_p / eps_feas, fmax(k.rel_d / eps_feas, k.rel_gap / eps_opt));
+    if (params.verbose)
+      printf("refinement round %d: %d FP32 iterations (reason %d, primal weight %.3g) -> FP64 "
+             "rel primal %.3e rel dual %.3e rel gap %.3e\n",
+             round, s.total_count(), r, s.primal_weight(), k.rel_p, k.rel_d, k.rel_gap);
+    if (round > 0 && err >= best_err) {
+      // the round did not improve the FP64 point: keep the previous one
+      k_rollback<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold);
+      launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
+      PDLP_LAUNCH_CHECK();
+      launches += 2;
+      break;
+    }
+    best_err = err;
+    kkt = k;
+    if (err < 1.0) {
+      reason = TERMINATION_REASON_OPTIMAL;
+      break;
+    }
+    if (r == TERMINATION_REASON_ITERATION_LIMIT || r == TERMINATION_REASON_TIME_LIMIT ||
+        iters >= limit) {
+      reason = r == TERMINATION_REASON_TIME_LIMIT ? r : TERMINATION_REASON_ITERATION_LIMIT;
+      break;
+    }
+  }
+  (void)linf;
+  double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  rep.inner_iterations = iters;
+  rep.kernel_launches = launches;
+  rep.seconds = seconds;
+  rep.kkt = kkt;
+  if (report) *report = rep;
+  if (ray_result) {
+    ray_result->total_count = (int)iters;
+    ray_result->cumulative_time_sec = seconds;
+    return ray_result;
+  }
+
+  auto *res = (cupdlpx_result_t *)calloc(1, sizeof(cupdlpx_result_t));
+  if (!res) throw std::bad_alloc();
+  res->primal_solution = (double *)malloc(sizeof(double) * (n ? n : 1));
+  res->dual_solution = (double *)malloc(sizeof(double) * (m ? m : 1));
+  res->reduced_cost = (double *)malloc(sizeof(double) * (n ? n : 1));
+  if (!res->primal_solution || !res->dual_solution || !res->reduced_cost) {
+    free(res->primal_solution);
+    free(res->dual_solution);
+    free(res->reduced_cost);
+    free(res);
+    throw std::bad_alloc();
+  }
+  if (n) {
+    PDLP_CUDA(cudaMemcpyAsync(res->primal_solution, xbar, vn * 8, cudaMemcpyDeviceToHost, st));
+    PDLP_CUDA(cudaMemcpyAsync(res->reduced_cost, rc, vn * 8, cudaMemcpyDeviceToHost, st));
+  }
+  if (m) PDLP_CUDA(cudaMemcpyAsync(res->dual_solution, ybar, vm * 8, cudaMemcpyDeviceToHost, st));
+  PDLP_CUDA(cudaStreamSynchronize(st));
+  res->num_variables = n;
+  res->num_constraints = m;
+  res->num_nonzeros = nnz;
+  res->num_reduced_variables = n;
+  res->num_reduced_constraints = m;
+  res->num_reduced_nonzeros = nnz;
+  res->total_count = (int)iters;
+  res->rescaling_time_sec = rescale_sec;
+  res->cumulative_time_sec = seconds;
+  res->absolute_primal_residual = kkt.abs_p;
+  res->relative_primal_residual = kkt.rel_p;
+  res->absolute_dual_residual = kkt.abs_d;
+  res->relative_dual_residual = kkt.rel_d;
+  res->primal_objective_value = kkt.pobj;
+  res->dual_objective_value = kkt.dobj;
+  res->objective_gap = kkt.gap;
+  res->relative_objective_gap = kkt.rel_gap;
+  res->termination_reason = (termination_reason_t)reason;
+  return res;
+}
+
+}  // namespace pdlp

@@ -1,4 +1,4 @@
-// solver.cu -- restarted Halpern PDHG on one GPU, FP64.
+// solver.cu -- restarted Halpern PDHG on one GPU (FP64 or FP32 iterates).
 //
 // Per iteration two kernels run (reference src/solver.cu:85-102):
 //   primal : g = A^T y (fused SpMV) -> x_hat = proj(x - tau (c - g)),
@@ -14,339 +14,46 @@
 // Evaluations, restarts, the fixed-point error and the termination test run
 // on the device at the iterations the reference schedules them
 // (reference src/solver.cu:58-103), so no iteration waits on the host.
+// Chunks of iterations are captured once as CUDA graphs and replayed.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
 #include <random>
 
-#include "solver.cuh"
+#include "iter_kernels.cuh"
 
 namespace pdlp {
 
-// ======================================================= SpMV epilogues
-// Epilogues without per-block scalars.
-#define PDLP_NO_BLOCK_SCALARS                        \
-  __device__ void prologue(double *) const {}        \
-  __device__ void bind(const double *) {}
-
-// Halpern weight w = (k+1)/(k+2), k = inner iteration count
-// (reference pdlp_core_op.cu:559-567), formed once per block.
-__device__ __forceinline__ void halpern_weight(const Ctl *c, int off, double *sc) {
-  int k = c->t_base + off - c->restart_t;
-  double w = (double)(k + 1) / (double)(k + 2);
-  sc[0] = w;
-  sc[1] = 1.0 - w;
-}
-
-template <bool MAJOR, bool FPE>
-struct PrimalEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = FPE ? 1 : 0;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  int off;
-  const double *xcur, *ycur;
-  double *xnext;
-  double tau, w, omw;
-  __device__ bool init() {
-    const Ctl *c = d.ctl;
-    if (c->done) return false;
-    tau = c->tau;
-    return true;
-  }
-  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
-  __device__ void bind(const double *sc) {
-    w = sc[0];
-    omw = sc[1];
-  }
-  __device__ double gather(int i) const { return ycur[i]; }
-  __device__ void row(int j, double s, double *acc) const {
-    double xc = xcur[j];
-    double t = xc - tau * (d.c[j] - s);
-    double xh = fmax(d.lv[j], fmin(t, d.uv[j]));
-    if (MAJOR) {
-      d.xhat[j] = xh;
-      d.lam[j] = (xh - t) / tau;
-    }
-    double xr = 2.0 * xh - xc;
-    d.xref[j] = xr;
-    if (FPE) {
-      double dd = xr - xc;
-      d.dx[j] = dd;
-      acc[0] += dd * dd;
-    }
-    double refl = d.rho_is_one ? xr : d.rho * xr + d.one_minus_rho * xc;
-    xnext[j] = w * refl + omw * d.x0[j];
-  }
-};
-
-template <bool MAJOR, bool FPE>
-struct DualEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = FPE ? 1 : 0;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  int off;
-  const double *ycur;
-  double *ynext;
-  double sigma, inv_sigma, w, omw;
-  __device__ bool init() {
-    const Ctl *c = d.ctl;
-    if (c->done) return false;
-    sigma = c->sigma;
-    inv_sigma = c->inv_sigma;
-    return true;
-  }
-  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
-  __device__ void bind(const double *sc) {
-    w = sc[0];
-    omw = sc[1];
-  }
-  __device__ double gather(int j) const { return d.xref[j]; }
-  __device__ void row(int i, double s, double *acc) const {
-    double yc = ycur[i];
-    // the reference divides by sigma; one reciprocal per launch instead
-    // (at most 1 ulp apart; an FP64 division costs ~10 FP64 issue slots)
-    double t = yc * inv_sigma - s;
-    double tp = fmax(-d.uc[i], fmin(t, -d.lc[i]));
-    double yh = (t - tp) * sigma;
-    if (MAJOR) d.yhat[i] = yh;
-    double yr = 2.0 * yh - yc;
-    if (FPE) {
-      double dd = yr - yc;
-      d.dy[i] = dd;
-      acc[0] += dd * dd;
-    }
-    double refl = d.rho_is_one ? yr : d.rho * yr + d.one_minus_rho * yc;
-    ynext[i] = w * refl + omw * d.y0[i];
-  }
-};
-
-// cross term <A^T dy, dx> of the fixed-point error (pdlp_core_op.cu:658-696)
-template <bool RESTART_ONLY>
-struct FpeEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 1;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() {
-    if (d.ctl->done) return false;
-    if (RESTART_ONLY && !d.ctl->do_restart) return false;
-    return true;
-  }
-  __device__ double gather(int i) const { return d.dy[i]; }
-  __device__ void row(int j, double s, double *acc) const { acc[0] += s * d.dx[j]; }
-};
-
-// KKT over A x_hat (utils.cu:503-531 constraint half)
-template <bool LINF>
-struct EvalAEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 2;
-  static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
-  Dev d;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() { return !d.ctl->done; }
-  __device__ double gather(int j) const { return d.xhat[j]; }
-  __device__ void row(int i, double s, double *acc) const {
-    double cl = fmax(d.lc[i], fmin(s, d.uc[i]));
-    double pr = (s - cl) * d.Dr[i];
-    acc[0] = LINF ? fmax(acc[0], fabs(pr)) : acc[0] + pr * pr;
-    double yh = d.yhat[i];
-    acc[1] += fmax(yh, 0.0) * d.lcf[i] + fmin(yh, 0.0) * d.ucf[i];
-  }
-};
-
-// KKT over A^T y_hat (utils.cu:503-531 variable half, plus objective dots)
-template <bool LINF>
-struct EvalATEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 3;
-  static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
-  Dev d;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() { return !d.ctl->done; }
-  __device__ double gather(int i) const { return d.yhat[i]; }
-  __device__ void row(int j, double s, double *acc) const {
-    double lam = d.lam[j];
-    double dr = (d.c[j] - s - lam) * d.Dc[j];
-    acc[0] = LINF ? fmax(acc[0], fabs(dr)) : acc[0] + dr * dr;
-    double xh = d.xhat[j];
-    acc[1] += d.c[j] * xh;
-    acc[2] += lam * xh;
-  }
-};
-
-__device__ __forceinline__ double ray_scale(const Ctl *c) {
-  double p = c->ray_primal_inf_norm;
-  return p > 0.0 ? 1.0 / p : 1.0;
-}
-
-// primal ray over A (utils.cu:561-572, :588-600)
-struct InfAEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 2;
-  static constexpr unsigned MAXMASK = 1u;
-  Dev d;
-  double sc;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() {  // runs twice per solve: a per-thread division is fine
-    if (d.ctl->done) return false;
-    sc = ray_scale(d.ctl);
-    return true;
-  }
-  __device__ double gather(int j) const { return sc * d.dx[j]; }
-  __device__ void row(int i, double s, double *acc) const {
-    double pi = (fmax(0.0, -s) * (double)isfinite(d.lc[i]) +
-                 fmax(0.0, s) * (double)isfinite(d.uc[i])) * d.Dr[i];
-    acc[0] = fmax(acc[0], fabs(pi));
-    double dy = d.dy[i];
-    acc[1] += fmax(dy, 0.0) * d.lcf[i] + fmin(dy, 0.0) * d.ucf[i];
-  }
-};
-
-// dual ray over A^T (utils.cu:574-586, :602-614; the slack slot holds A^T dy
-// as in the reference call at utils.cu:772-776)
-struct InfATEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 3;
-  static constexpr unsigned MAXMASK = 2u;
-  Dev d;
-  double sc;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() {
-    if (d.ctl->done) return false;
-    sc = ray_scale(d.ctl);
-    return true;
-  }
-  __device__ double gather(int i) const { return d.dy[i]; }
-  __device__ void row(int j, double s, double *acc) const {
-    double ns = -s;
-    acc[0] += fmax(ns, 0.0) * d.lvf[j] + fmin(ns, 0.0) * d.uvf[j];
-    double di = (fmax(0.0, ns) * (double)!isfinite(d.lv[j]) -
-                 fmin(0.0, ns) * (double)!isfinite(d.uv[j])) * d.Dc[j];
-    acc[1] = fmax(acc[1], fabs(di));
-    acc[2] += d.c[j] * (sc * d.dx[j]);
-  }
-};
-
-// reduced cost (pdlp_core_op.cu:31-40)
-struct ReducedCostEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 0;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() { return true; }
-  __device__ double gather(int i) const { return d.yhat[i]; }
-  __device__ void row(int j, double s, double *) const {
-    d.auxn[j] = (d.c[j] - s) * d.Dc[j] / d.ob;
-  }
-};
-
-// power method: g = A^T (inv * v)   (utils.cu:127-136)
-struct PowAtEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 0;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  const double *v;
-  double inv;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() {
-    if (d.ctl->pm_done) return false;
-    inv = d.ctl->pm_inv_norm;
-    return true;
-  }
-  __device__ double gather(int i) const { return inv * v[i]; }
-  __device__ void row(int j, double s, double *) const { d.pm_g[j] = s; }
-};
-
-// power method: v' = A g, sum q.v', sum v'^2   (utils.cu:138-144)
-struct PowAEpi {
-  using val_t = double;
-  using acc_t = double;
-  static constexpr int NF = 2;
-  static constexpr unsigned MAXMASK = 0;
-  Dev d;
-  const double *v;
-  double *vnext;
-  double inv;
-  PDLP_NO_BLOCK_SCALARS
-  __device__ bool init() {
-    if (d.ctl->pm_done) return false;
-    inv = d.ctl->pm_inv_norm;
-    return true;
-  }
-  __device__ double gather(int j) const { return d.pm_g[j]; }
-  __device__ void row(int i, double s, double *acc) const {
-    vnext[i] = s;
-    double q = inv * v[i];
-    acc[0] += q * s;
-    acc[1] += s * s;
-  }
-};
-
-// step sizes derived from eta and omega (reference pdlp_core_op.cu:512, :545)
-__device__ __forceinline__ void set_steps(Ctl *c) {
-  c->tau = c->step_size / c->primal_weight;
-  c->sigma = c->step_size * c->primal_weight;
-  c->inv_sigma = 1.0 / c->sigma;
-}
-__global__ void k_set_steps(Ctl *c) { set_steps(c); }
-
-// ================================================================ launch
-template <class Epi>
-void launch_spmv(const DevCsr &M, const Epi &epi, double *part, double *lpart,
-                 cudaStream_t st) {
-  if (M.plan.nblk == 0) return;
-  if (M.plan.tile == 2048)
-    spmv_fused<2048, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
-                                                             part, lpart, epi);
-  else if (M.plan.tile == 1024)
-    spmv_fused<1024, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
-                                                             part, lpart, epi);
-  else
-    spmv_fused<512, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
-                                                            part, lpart, epi);
-  PDLP_LAUNCH_CHECK();
-}
+// Evaluation modes of k_eval_fin.
+enum EvalMode { kEvalCheck = 0, kEvalIterLimit = 1, kEvalOnly = 2 };
 
 // ======================================================= element kernels
 __global__ void k_set_tbase(Ctl *ctl, int t) { ctl->t_base = t; }
-
 __global__ void k_loop_start(Ctl *ctl) { ctl->t_start_ns = global_ns(); }
+__global__ void k_set_steps(Ctl *c) { set_steps(c); }
 
 // Ray projection + infinity norms (utils.cu:533-559, :744-748)
-__global__ void __launch_bounds__(kThreads) k_ray_project(Dev d) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_ray_project(Dev<T> d) {
   if (d.ctl->done) return;
   __shared__ double red[24];
   double a[2] = {0.0, 0.0};
   long stride = (long)gridDim.x * kThreads;
   for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
-    double v = d.dx[j];
-    if (isfinite(d.lv[j])) v = fmax(v, 0.0);
-    if (isfinite(d.uv[j])) v = fmin(v, 0.0);
+    T v = d.dx[j];
+    if (isfinite(d.lv[j])) v = fmax(v, T(0));
+    if (isfinite(d.uv[j])) v = fmin(v, T(0));
     d.dx[j] = v;
-    a[0] = fmax(a[0], fabs(v));
+    a[0] = fmax(a[0], fabs((double)v));
   }
   for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
-    double v = d.dy[i];
-    if (!isfinite(d.lc[i])) v = fmin(v, 0.0);
-    if (!isfinite(d.uc[i])) v = fmax(v, 0.0);
+    T v = d.dy[i];
+    if (!isfinite(d.lc[i])) v = fmin(v, T(0));
+    if (!isfinite(d.uc[i])) v = fmax(v, T(0));
     d.dy[i] = v;
-    a[1] = fmax(a[1], fabs(v));
+    a[1] = fmax(a[1], fabs((double)v));
   }
   block_reduce_fields<2, 3u>(a, red);
   if (threadIdx.x == 0) {
@@ -355,7 +62,8 @@ __global__ void __launch_bounds__(kThreads) k_ray_project(Dev d) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_ray_project_fin(Dev d) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_ray_project_fin(Dev<T> d) {
   if (d.ctl->done) return;
   __shared__ double sm[32];
   double p = block_fold<true>(d.p_i0, d.ew_grid, sm);
@@ -367,22 +75,22 @@ __global__ void __launch_bounds__(kThreads) k_ray_project_fin(Dev d) {
 }
 
 // Restart copy + distances (pdlp_core_op.cu:577-591, :621-632)
-__global__ void __launch_bounds__(kThreads)
-    k_restart(Dev d, double *xcur, double *ycur) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_restart(Dev<T> d, T *xcur, T *ycur) {
   if (d.ctl->done || !d.ctl->do_restart) return;
   __shared__ double red[24];
   double a[2] = {0.0, 0.0};
   long stride = (long)gridDim.x * kThreads;
   for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
-    double xh = d.xhat[j];
-    double dd = xh - d.x0[j];
+    T xh = d.xhat[j];
+    double dd = (double)xh - (double)d.x0[j];
     a[0] += dd * dd;
     d.x0[j] = xh;
     xcur[j] = xh;
   }
   for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
-    double yh = d.yhat[i];
-    double dd = yh - d.y0[i];
+    T yh = d.yhat[i];
+    double dd = (double)yh - (double)d.y0[i];
     a[1] += dd * dd;
     d.y0[i] = yh;
     ycur[i] = yh;
@@ -395,7 +103,8 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // PID primal-weight update (pdlp_core_op.cu:593-619)
-__global__ void __launch_bounds__(kThreads) k_restart_fin(Dev d, int off) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_restart_fin(Dev<T> d, int off) {
   Ctl *c = d.ctl;
   if (c->done || !c->do_restart) return;
   __shared__ double sm[32];
@@ -428,7 +137,8 @@ __global__ void __launch_bounds__(kThreads) k_restart_fin(Dev d, int off) {
 
 // Fixed-point error (pdlp_core_op.cu:677-695) + restart bookkeeping
 // (solver.cu:89-95)
-__global__ void __launch_bounds__(kThreads) k_fpe_fin(Dev d, int restart_only) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_fpe_fin(Dev<T> d, int restart_only) {
   Ctl *c = d.ctl;
   if (c->done) return;
   if (restart_only && !c->do_restart) return;
@@ -450,8 +160,9 @@ __global__ void __launch_bounds__(kThreads) k_fpe_fin(Dev d, int restart_only) {
 
 // Evaluation: KKT scalars, optional ray statistics, termination test,
 // restart decision, trace record (utils.cu:639-813, :239-293; solver.cu:59-83)
+template <class T>
 __global__ void __launch_bounds__(kThreads)
-    k_eval_fin(Dev d, int off, int infeas, int restart_check, int final_eval) {
+    k_eval_fin(Dev<T> d, int off, int infeas, int restart_check, int mode) {
   Ctl *c = d.ctl;
   if (c->done) return;
   __shared__ double sm[32];
@@ -476,12 +187,18 @@ __global__ void __launch_bounds__(kThreads)
   const double cbo = d.cb * d.ob;
   c->abs_primal_res = (L ? pr : sqrt(pr)) / d.cb;
   c->abs_dual_res = (L ? dr : sqrt(dr)) / d.ob;
-  c->primal_obj = cx / cbo + d.c0;
-  c->dual_obj = (lx + qsum) / cbo + d.c0;
+  if (d.shifted) {  // terms already in original units
+    c->primal_obj = cx + d.oc0;
+    c->dual_obj = lx + qsum + d.oc0;
+  } else {
+    c->primal_obj = cx / cbo + d.c0;
+    c->dual_obj = (lx + qsum) / cbo + d.c0;
+  }
   c->rel_primal_res = c->abs_primal_res / (1.0 + d.bnorm);
   c->rel_dual_res = c->abs_dual_res / (1.0 + d.cnorm);
   c->gap = fabs(c->primal_obj - c->dual_obj);
   c->rel_gap = c->gap / (1.0 + fabs(c->primal_obj) + fabs(c->dual_obj));
+  if (mode == kEvalOnly) return;
   if (infeas) {
     c->primal_ray_obj = i2c / cbo;
     c->dual_ray_obj = (i1sum + i2sum) / cbo;
@@ -498,7 +215,20 @@ __global__ void __launch_bounds__(kThreads)
   }
   c->cum_time = (double)(global_ns() - c->t_start_ns) * 1e-9;
   int reason = TERMINATION_REASON_UNSPECIFIED;
-  if (final_eval) {
+  bool stalled = false;
+  if (d.stall_min > 0 && mode == kEvalCheck) {
+    // best-iterate snapshot and stall rule of the refinement rounds
+    double err = fmax(c->rel_primal_res, fmax(c->rel_dual_res, c->rel_gap));
+    c->snap_now = err < c->snap_err ? 1 : 0;
+    if (c->snap_now) c->snap_err = err;
+    if (err < 0.9 * c->best_err) {
+      c->best_err = err;
+      c->best_err_t = t;
+    } else if (t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
+      stalled = true;
+    }
+  }
+  if (mode == kEvalIterLimit) {
     reason = TERMINATION_REASON_ITERATION_LIMIT;
   } else if (c->rel_dual_res < d.eps_feas && c->rel_primal_res < d.eps_feas &&
              c->rel_gap < d.eps_opt) {
@@ -510,6 +240,8 @@ __global__ void __launch_bounds__(kThreads)
     reason = TERMINATION_REASON_DUAL_INFEASIBLE;
   } else if (c->cum_time >= d.time_limit) {
     reason = TERMINATION_REASON_TIME_LIMIT;
+  } else if (stalled) {
+    reason = kReasonStalled;
   }
   if (d.trace && c->trace_len < d.trace_cap) {
     double *r = d.trace + (long)c->trace_len * 10;
@@ -554,8 +286,21 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// ---- power method element kernels (utils.cu:107-153)
-__global__ void __launch_bounds__(kThreads) k_pm_norm(Dev d, const double *v) {
+// Copy the evaluated iterate into the snapshot when it is the best so far.
+template <class T>
+__global__ void k_snapshot(Dev<T> d) {
+  if (!d.ctl->snap_now) return;
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
+    d.bx[j] = d.xhat[j];
+    d.bl[j] = d.lam[j];
+  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
+    d.by[i] = d.yhat[i];
+}
+
+// ---- power method element kernels (utils.cu:107-153), FP64
+__global__ void __launch_bounds__(kThreads) k_pm_norm(PowDev d, const double *v) {
   if (d.ctl->pm_done) return;
   __shared__ double red[16];
   double a[1] = {0.0};
@@ -566,14 +311,14 @@ __global__ void __launch_bounds__(kThreads) k_pm_norm(Dev d, const double *v) {
   if (threadIdx.x == 0) d.p_pr[blockIdx.x] = a[0];
 }
 
-__global__ void __launch_bounds__(kThreads) k_pm_norm_fin(Dev d) {
+__global__ void __launch_bounds__(kThreads) k_pm_norm_fin(PowDev d) {
   if (d.ctl->pm_done) return;
   __shared__ double sm[32];
   double s = block_fold<false>(d.p_pr, d.ew_grid, sm);
   if (threadIdx.x == 0) d.ctl->pm_inv_norm = 1.0 / sqrt(s);
 }
 
-__global__ void __launch_bounds__(kThreads) k_pm_dot_fin(Dev d) {
+__global__ void __launch_bounds__(kThreads) k_pm_dot_fin(PowDev d) {
   Ctl *c = d.ctl;
   if (c->pm_done) return;
   __shared__ double sm[32];
@@ -586,7 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_pm_dot_fin(Dev d) {
 }
 
 __global__ void __launch_bounds__(kThreads)
-    k_pm_resid(Dev d, const double *v, const double *vnext) {
+    k_pm_resid(PowDev d, const double *v, const double *vnext) {
   if (d.ctl->pm_done) return;
   __shared__ double red[16];
   double inv = d.ctl->pm_inv_norm, ns = -d.ctl->pm_sigma_sq;
@@ -601,7 +346,7 @@ __global__ void __launch_bounds__(kThreads)
   if (threadIdx.x == 0) d.p_pr[blockIdx.x] = a[0];
 }
 
-__global__ void __launch_bounds__(kThreads) k_pm_resid_fin(Dev d) {
+__global__ void __launch_bounds__(kThreads) k_pm_resid_fin(PowDev d) {
   Ctl *c = d.ctl;
   if (c->pm_done) return;
   __shared__ double sm[32];
@@ -619,50 +364,74 @@ __global__ void __launch_bounds__(kThreads) k_pm_resid_fin(Dev d) {
   }
 }
 
-// Unscale (pdlp_core_op.cu:464-480)
-__global__ void k_unscale(Dev d) {
+// Unscale (pdlp_core_op.cu:464-480) into FP64 outputs; the dual slack maps
+// back like the reduced cost (times Dc / ob).
+template <class T>
+__global__ void k_unscale(Dev<T> d, double *x, double *y, double *lam) {
   long stride = (long)gridDim.x * blockDim.x;
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride)
-    d.xhat[j] = d.xhat[j] / d.Dc[j] / d.cb;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
+    x[j] = (double)d.xhat[j] / d.Dc[j] / d.cb;
+    if (lam) lam[j] = (double)d.lam[j] * d.Dc[j] / d.ob;
+  }
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
-    d.yhat[i] = d.yhat[i] / d.Dr[i] / d.ob;
+    y[i] = (double)d.yhat[i] / d.Dr[i] / d.ob;
+}
+
+// Scale an original-units point into this solve's scaled space.
+template <class T>
+__global__ void k_scale_point(Dev<T> d, const double *x, const double *y, const double *lam) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
+    d.xhat[j] = (T)(x[j] * d.Dc[j] * d.cb);
+    d.lam[j] = (T)(lam[j] * d.ob / d.Dc[j]);
+  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
+    d.yhat[i] = (T)(y[i] * d.Dr[i] * d.ob);
 }
 
 // Finite copies of the scaled bounds (pdlp_core_op.cu:203-230)
-__global__ void k_finite_copies(int n, int m, const double *lv, const double *uv,
-                                const double *lc, const double *uc, double *lvf,
-                                double *uvf, double *lcf, double *ucf) {
+template <class T>
+__global__ void k_finite_copies(int n, int m, const T *lv, const T *uv, const T *lc,
+                                const T *uc, T *lvf, T *uvf, T *lcf, T *ucf) {
   long stride = (long)gridDim.x * blockDim.x;
   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
-    lvf[j] = isfinite(lv[j]) ? lv[j] : 0.0;
-    uvf[j] = isfinite(uv[j]) ? uv[j] : 0.0;
+    lvf[j] = isfinite(lv[j]) ? lv[j] : T(0);
+    uvf[j] = isfinite(uv[j]) ? uv[j] : T(0);
   }
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
-    lcf[i] = isfinite(lc[i]) ? lc[i] : 0.0;
-    ucf[i] = isfinite(uc[i]) ? uc[i] : 0.0;
+    lcf[i] = isfinite(lc[i]) ? lc[i] : T(0);
+    ucf[i] = isfinite(uc[i]) ? uc[i] : T(0);
   }
 }
 
 // Warm start scaling (pdlp_core_op.cu:174-201)
+template <class T>
 __global__ void k_warm_start(int n, int m, const double *xs, const double *ys,
-                             const double *Dc, const double *Dr, double cb, double ob,
-                             double *x0, double *x, double *xhat, double *y0, double *y,
-                             double *yhat) {
+                             const double *Dc, const double *Dr, double cb, double ob, T *x0,
+                             T *x, T *xhat, T *y0, T *y, T *yhat) {
   long stride = (long)gridDim.x * blockDim.x;
   if (xs)
     for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
-      double v = xs[j] * Dc[j] * cb;
+      T v = (T)(xs[j] * Dc[j] * cb);
       x0[j] = v;
       x[j] = v;
       xhat[j] = v;
     }
   if (ys)
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
-      double v = ys[i] * Dr[i] * ob;
+      T v = (T)(ys[i] * Dr[i] * ob);
       y0[i] = v;
       y[i] = v;
       yhat[i] = v;
     }
+}
+
+// FP64 -> T copy (rounding to nearest)
+template <class T>
+__global__ void k_convert(long n, const double *__restrict__ src, T *__restrict__ dst) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride)
+    dst[i] = (T)src[i];
 }
 
 // ============================================================ host side
@@ -682,7 +451,10 @@ struct Arena {
 
 struct Sizer {
   size_t bytes = 0;
-  void add(size_t b) { bytes += align256(b + 1); }
+  template <class T>
+  void add(size_t count) {
+    bytes += align256(count * sizeof(T) + 1);
+  }
 };
 }  // namespace
 
@@ -777,14 +549,14 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   }
   const size_t vn = n, vm = m;
   Sizer z;
-  z.add((vm + 1) * 4); z.add((size_t)nnz * 4); z.add((size_t)nnz * 8);
-  z.add((vn + 1) * 4); z.add((size_t)nnz * 4); z.add((size_t)nnz * 8);
-  z.add(blkA.size() * 16); z.add(lrA.size() * 8);
-  z.add(blkT.size() * 16); z.add(lrT.size() * 8);
-  for (int i = 0; i < 3; ++i) z.add(vn * 8);
-  for (int i = 0; i < 2; ++i) z.add(vm * 8);
-  if (prob->primal_start) z.add(vn * 8);
-  if (prob->dual_start) z.add(vm * 8);
+  z.add<int>(vm + 1); z.add<int>(nnz); z.add<double>(nnz);
+  z.add<int>(vn + 1); z.add<int>(nnz); z.add<double>(nnz);
+  z.add<int4>(blkA.size()); z.add<int2>(lrA.size());
+  z.add<int4>(blkT.size()); z.add<int2>(lrT.size());
+  for (int i = 0; i < 3; ++i) z.add<double>(vn);
+  for (int i = 0; i < 2; ++i) z.add<double>(vm);
+  if (prob->primal_start) z.add<double>(vn);
+  if (prob->dual_start) z.add<double>(vm);
   PDLP_CUDA(cudaMalloc(&P->arena, z.bytes));
   P->bytes = z.bytes;
   Arena ar{(char *)P->arena, 0};
@@ -839,69 +611,104 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   return P.release();
 }
 
-Solve::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
-             int trace_cap)
+template <class T>
+Solve<T>::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
+                int trace_cap)
     : p_(params), st_(stream), P_(prob), trace_cap_(trace_cap) {
   alloc();
 }
 
-Solve::~Solve() {
+template <class T>
+Solve<T>::~Solve() {
+  if (snap_mem_) cudaFree(snap_mem_);
   for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
   for (auto g : raw_graphs_) cudaGraphDestroy(g);
   if (arena_) cudaFree(arena_);
   if (hflag_) cudaFreeHost(hflag_);
 }
 
-void Solve::alloc() {
+template <class T>
+void Solve<T>::alloc() {
+  constexpr bool F64 = sizeof(T) == 8;
   const int n = P_.n, m = P_.m, nnz = P_.nnz;
   const int ew = grid_for((long)n + m, 4);
   const size_t vn = n, vm = m;
   const size_t nbA = P_.A.plan.nblk, nbT = P_.AT.plan.nblk;
   const size_t nlA = P_.A.plan.nlong, nlT = P_.AT.plan.nlong;
   Sizer z;
-  z.add((size_t)nnz * 8); z.add((size_t)nnz * 8);           // scaled values
-  z.add(nlA * 4); z.add(nbA * 8); z.add(nlT * 4); z.add(nbT * 8);  // per-solve plan scratch
-  for (int i = 0; i < 6; ++i) z.add(vn * 8);  // c lv uv lvf uvf Dc
-  for (int i = 0; i < 5; ++i) z.add(vm * 8);  // lc uc lcf ucf Dr
-  for (int i = 0; i < 8; ++i) z.add(vn * 8);  // x[2] x0 xref xhat lam dx auxn
-  for (int i = 0; i < 6; ++i) z.add(vm * 8);  // y[2] y0 yhat dy auxm
-  z.add(vm * 8); z.add(vm * 8); z.add(vn * 8);  // power v[2], g
+  z.add<double>(nnz); z.add<double>(nnz);                      // FP64 scaled values
+  if (!F64) { z.add<T>(nnz); z.add<T>(nnz); }                  // iteration values
+  z.add<unsigned>(nlA); z.add<double>(nbA); z.add<unsigned>(nlT); z.add<double>(nbT);
+  for (int i = 0; i < 3; ++i) z.add<double>(vn);               // c lv uv (FP64 scaled)
+  for (int i = 0; i < 2; ++i) z.add<double>(vm);               // lc uc
+  z.add<double>(vn); z.add<double>(vm);                        // Dc Dr
+  if (!F64) {
+    for (int i = 0; i < 3; ++i) z.add<T>(vn);
+    for (int i = 0; i < 2; ++i) z.add<T>(vm);
+  }
+  for (int i = 0; i < 2; ++i) z.add<T>(vn);                    // lvf uvf
+  for (int i = 0; i < 2; ++i) z.add<T>(vm);                    // lcf ucf
+  for (int i = 0; i < 8; ++i) z.add<T>(vn);                    // x[2] x0 xref xhat lam dx auxn
+  for (int i = 0; i < 6; ++i) z.add<T>(vm);                    // y[2] y0 yhat dy auxm
+  z.add<double>(vm); z.add<double>(vm); z.add<double>(vn);     // power v[2], g
+  z.add<double>(vn); z.add<double>(vm); z.add<double>(vn);     // FP64 outputs x, y, rc/lam
   size_t pa = nbA + nlA + 2, pt = nbT + nlT + 2;
-  z.add(pt * 8); z.add(pa * 8); z.add(pt * 8);  // pstep dstep fpe
-  z.add(pa * 16); z.add(pt * 24);               // e1 e2
-  z.add((size_t)ew * 16);                       // i0
-  z.add(pa * 16); z.add(pt * 24);               // i1 i2
-  z.add((size_t)ew * 16);                       // rs
-  z.add(pa * 16); z.add((size_t)ew * 8);        // pa pr
-  z.add((size_t)kMiscPart * 8);
-  z.add(sizeof(Ctl)); z.add((size_t)trace_cap_ * 80 + 8);
+  z.add<double>(pt); z.add<double>(pa); z.add<double>(pt);    // pstep dstep fpe
+  z.add<double>(pa * 2); z.add<double>(pt * 3);               // e1 e2
+  z.add<double>((size_t)ew * 2);                               // i0
+  z.add<double>(pa * 2); z.add<double>(pt * 3);               // i1 i2
+  z.add<double>((size_t)ew * 2);                               // rs
+  z.add<double>(pa * 2); z.add<double>((size_t)ew);           // power partials
+  z.add<double>((size_t)kMiscPart);
+  z.add<Ctl>(1); z.add<double>((size_t)trace_cap_ * 10 + 1);
   PDLP_CUDA(cudaMalloc(&arena_, z.bytes));
   Arena ar{(char *)arena_, 0};
 
-  auto mat = [&](DevCsr &W, const DevCsr &S) {
+  auto mat64 = [&](DevCsr &W, const DevCsr &S) {
     W = S;
     W.val = ar.take<double>(nnz);
     W.plan.lcnt = ar.take<unsigned>(S.plan.nlong);
     W.plan.lsum = ar.take<double>(S.plan.nblk);
-    if (S.plan.nlong)
-      PDLP_CUDA(cudaMemsetAsync(W.plan.lcnt, 0, (size_t)S.plan.nlong * 4, st_));
+    if (S.plan.nlong) PDLP_CUDA(cudaMemsetAsync(W.plan.lcnt, 0, (size_t)S.plan.nlong * 4, st_));
   };
-  mat(A_, P_.A);
-  mat(AT_, P_.AT);
+  mat64(A64_, P_.A);
+  mat64(AT64_, P_.AT);
+  auto matT = [&](DevCsrT<T> &W, const DevCsr &S64) {
+    W.rows = S64.rows;
+    W.cols = S64.cols;
+    W.nnz = S64.nnz;
+    W.ptr = S64.ptr;
+    W.col = S64.col;
+    W.plan = S64.plan;  // shares the per-solve scratch of the FP64 copy
+    if constexpr (F64) W.val = (T *)S64.val;
+    else W.val = ar.take<T>(nnz);
+  };
+  matT(A_, A64_);
+  matT(AT_, AT64_);
 
-  Dev &d = d_;
+  Dev<T> &d = d_;
   d.n = n;
   d.m = m;
-  d.c = ar.take<double>(vn); d.lv = ar.take<double>(vn); d.uv = ar.take<double>(vn);
-  d.lvf = ar.take<double>(vn); d.uvf = ar.take<double>(vn); d.Dc = ar.take<double>(vn);
-  d.lc = ar.take<double>(vm); d.uc = ar.take<double>(vm); d.lcf = ar.take<double>(vm);
-  d.ucf = ar.take<double>(vm); d.Dr = ar.take<double>(vm);
-  d.x[0] = ar.take<double>(vn); d.x[1] = ar.take<double>(vn); d.x0 = ar.take<double>(vn);
-  d.xref = ar.take<double>(vn); d.xhat = ar.take<double>(vn); d.lam = ar.take<double>(vn);
-  d.dx = ar.take<double>(vn); d.auxn = ar.take<double>(vn);
-  d.y[0] = ar.take<double>(vm); d.y[1] = ar.take<double>(vm); d.y0 = ar.take<double>(vm);
-  d.yhat = ar.take<double>(vm); d.dy = ar.take<double>(vm); d.auxm = ar.take<double>(vm);
-  d.pm_v[0] = ar.take<double>(vm); d.pm_v[1] = ar.take<double>(vm); d.pm_g = ar.take<double>(vn);
+  c64_ = ar.take<double>(vn); lv64_ = ar.take<double>(vn); uv64_ = ar.take<double>(vn);
+  lc64_ = ar.take<double>(vm); uc64_ = ar.take<double>(vm);
+  d.Dc = ar.take<double>(vn);
+  d.Dr = ar.take<double>(vm);
+  if constexpr (F64) {
+    d.c = (const T *)c64_; d.lv = (const T *)lv64_; d.uv = (const T *)uv64_;
+    d.lc = (const T *)lc64_; d.uc = (const T *)uc64_;
+  } else {
+    d.c = ar.take<T>(vn); d.lv = ar.take<T>(vn); d.uv = ar.take<T>(vn);
+    d.lc = ar.take<T>(vm); d.uc = ar.take<T>(vm);
+  }
+  d.lvf = ar.take<T>(vn); d.uvf = ar.take<T>(vn);
+  d.lcf = ar.take<T>(vm); d.ucf = ar.take<T>(vm);
+  d.x[0] = ar.take<T>(vn); d.x[1] = ar.take<T>(vn); d.x0 = ar.take<T>(vn);
+  d.xref = ar.take<T>(vn); d.xhat = ar.take<T>(vn); d.lam = ar.take<T>(vn);
+  d.dx = ar.take<T>(vn); d.auxn = ar.take<T>(vn);
+  d.y[0] = ar.take<T>(vm); d.y[1] = ar.take<T>(vm); d.y0 = ar.take<T>(vm);
+  d.yhat = ar.take<T>(vm); d.dy = ar.take<T>(vm); d.auxm = ar.take<T>(vm);
+  pw_.v[0] = ar.take<double>(vm); pw_.v[1] = ar.take<double>(vm); pw_.g = ar.take<double>(vn);
+  outx_ = ar.take<double>(vn); outy_ = ar.take<double>(vm); outl_ = ar.take<double>(vn);
   d.nblkA = (int)nbA; d.nlongA = (int)nlA; d.nblkT = (int)nbT; d.nlongT = (int)nlT;
   d.ew_grid = ew;
   auto split = [&](double *&p, double *&lp, size_t nb, size_t nl, int nf) {
@@ -918,8 +725,8 @@ void Solve::alloc() {
   split(d.p_i1, d.lp_i1, nbA, nlA, 2);
   split(d.p_i2, d.lp_i2, nbT, nlT, 3);
   d.p_rs = ar.take<double>((size_t)ew * 2);
-  split(d.p_pa, d.lp_pa, nbA, nlA, 2);
-  d.p_pr = ar.take<double>((size_t)ew);
+  split(pw_.p_pa, pw_.lp_pa, nbA, nlA, 2);
+  pw_.p_pr = ar.take<double>((size_t)ew);
   d.p_misc = ar.take<double>((size_t)kMiscPart);
   d.ctl = ar.take<Ctl>(1);
   d.trace = trace_cap_ > 0 ? ar.take<double>((size_t)trace_cap_ * 10) : nullptr;
@@ -931,13 +738,29 @@ void Solve::alloc() {
   HostFlag *dflag = nullptr;
   PDLP_CUDA(cudaHostGetDevicePointer((void **)&dflag, hflag_, 0));
   d.hflag = dflag;
+
+  pw_.n = n;
+  pw_.m = m;
+  pw_.ctl = d.ctl;
+  pw_.hflag = dflag;
+  pw_.nblkA = (int)nbA;
+  pw_.nlongA = (int)nlA;
+  pw_.ew_grid = ew;
 }
 
-void Solve::prepare() {
-  Dev &d = d_;
+template <class T>
+void Solve<T>::prepare() {
+  Dev<T> &d = d_;
   const int n = d.n, m = d.m, nnz = P_.nnz;
   auto t0 = std::chrono::steady_clock::now();
   d.c0 = P_.c0;
+  d.shifted = P_.shift_x != nullptr;
+  d.sx = P_.shift_x;
+  d.sy = P_.shift_y;
+  d.oc = P_.orig_c;
+  d.olcf = P_.orig_lcf;
+  d.oucf = P_.orig_ucf;
+  d.oc0 = P_.orig_c0;
   d.rho = p_.reflection_coefficient;
   d.one_minus_rho = 1.0 - d.rho;
   d.rho_is_one = d.rho == 1.0;
@@ -957,32 +780,42 @@ void Solve::prepare() {
   d.ki = p_.restart_params.k_i;
   d.kd = p_.restart_params.k_d;
   d.ismooth = p_.restart_params.i_smooth;
-  d.sv_tol = p_.sv_tol;
+  pw_.sv_tol = p_.sv_tol;
   auto d2d = [&](const void *dst, const void *src, size_t b) {
     if (b) PDLP_CUDA(cudaMemcpyAsync((void *)dst, src, b, cudaMemcpyDeviceToDevice, st_));
   };
-  d2d(A_.val, P_.A.val, (size_t)nnz * 8);
-  d2d(AT_.val, P_.AT.val, (size_t)nnz * 8);
-  d2d(d.c, P_.c, (size_t)n * 8);
-  d2d(d.lv, P_.lv, (size_t)n * 8);
-  d2d(d.uv, P_.uv, (size_t)n * 8);
-  d2d(d.lc, P_.lc, (size_t)m * 8);
-  d2d(d.uc, P_.uc, (size_t)m * 8);
-  gpu_rescale(p_, A_, AT_, (double *)d.c, (double *)d.lv, (double *)d.uv, (double *)d.lc,
-              (double *)d.uc, (double *)d.Dr, (double *)d.Dc, &d.cb, &d.ob, d.auxn, d.auxm,
-              d.p_misc, st_);
-  rescale_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  d2d(A64_.val, P_.A.val, (size_t)nnz * 8);
+  d2d(AT64_.val, P_.AT.val, (size_t)nnz * 8);
+  d2d(c64_, P_.c, (size_t)n * 8);
+  d2d(lv64_, P_.lv, (size_t)n * 8);
+  d2d(uv64_, P_.uv, (size_t)n * 8);
+  d2d(lc64_, P_.lc, (size_t)m * 8);
+  d2d(uc64_, P_.uc, (size_t)m * 8);
+  gpu_rescale(p_, A64_, AT64_, c64_, lv64_, uv64_, lc64_, uc64_, (double *)d.Dr,
+              (double *)d.Dc, &d.cb, &d.ob, outx_, outy_, d.p_misc, st_);
   int g = grid_for((long)n + m);
-  k_finite_copies<<<g, kThreads, 0, st_>>>(n, m, d.lv, d.uv, d.lc, d.uc, (double *)d.lvf,
-                                           (double *)d.uvf, (double *)d.lcf, (double *)d.ucf);
+  if constexpr (sizeof(T) != 8) {
+    int gz = grid_for(nnz);
+    k_convert<T><<<gz, kThreads, 0, st_>>>(nnz, A64_.val, A_.val);
+    k_convert<T><<<gz, kThreads, 0, st_>>>(nnz, AT64_.val, AT_.val);
+    int gn = grid_for(n), gm = grid_for(m);
+    k_convert<T><<<gn, kThreads, 0, st_>>>(n, c64_, (T *)d.c);
+    k_convert<T><<<gn, kThreads, 0, st_>>>(n, lv64_, (T *)d.lv);
+    k_convert<T><<<gn, kThreads, 0, st_>>>(n, uv64_, (T *)d.uv);
+    k_convert<T><<<gm, kThreads, 0, st_>>>(m, lc64_, (T *)d.lc);
+    k_convert<T><<<gm, kThreads, 0, st_>>>(m, uc64_, (T *)d.uc);
+    PDLP_LAUNCH_CHECK();
+  }
+  k_finite_copies<T><<<g, kThreads, 0, st_>>>(n, m, d.lv, d.uv, d.lc, d.uc, (T *)d.lvf,
+                                              (T *)d.uvf, (T *)d.lcf, (T *)d.ucf);
   PDLP_LAUNCH_CHECK();
-  for (double *p : {d.x[0], d.x[1], d.x0, d.xref, d.xhat, d.lam, d.dx})
-    if (n) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)n * 8, st_));
-  for (double *p : {d.y[0], d.y[1], d.y0, d.yhat, d.dy})
-    if (m) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)m * 8, st_));
+  for (T *p : {d.x[0], d.x[1], d.x0, d.xref, d.xhat, d.lam, d.dx})
+    if (n) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)n * sizeof(T), st_));
+  for (T *p : {d.y[0], d.y[1], d.y0, d.yhat, d.dy})
+    if (m) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)m * sizeof(T), st_));
   if (P_.xs || P_.ys) {
-    k_warm_start<<<g, kThreads, 0, st_>>>(n, m, P_.xs, P_.ys, d.Dc, d.Dr, d.cb, d.ob, d.x0,
-                                          d.x[0], d.xhat, d.y0, d.y[0], d.yhat);
+    k_warm_start<T><<<g, kThreads, 0, st_>>>(n, m, P_.xs, P_.ys, d.Dc, d.Dr, d.cb, d.ob, d.x0,
+                                             d.x[0], d.xhat, d.y0, d.y[0], d.yhat);
     PDLP_LAUNCH_CHECK();
   }
   Ctl c0;
@@ -990,15 +823,23 @@ void Solve::prepare() {
   c0.best_gap = INFINITY;
   c0.last_trial_fixed_point_error = INFINITY;
   c0.reason = TERMINATION_REASON_UNSPECIFIED;
+  c0.step_size = 1.0;
+  c0.primal_weight = 1.0;
+  c0.best_primal_weight = 1.0;
+  c0.tau = c0.sigma = c0.inv_sigma = 1.0;
+  c0.best_err = INFINITY;
+  c0.snap_err = INFINITY;
   PDLP_CUDA(cudaMemcpyAsync(d.ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
   hflag_->done = 0;
   hflag_->pm_done = 0;
+  rescale_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void Solve::power_method() {
-  Dev &d = d_;
-  const int m = d.m;
+template <class T>
+void Solve<T>::power_method() {
+  PowDev &w = pw_;
+  const int m = w.m;
   // start vector: m draws of N(0,1) from a fresh mt19937(1), like the
   // reference's first solve in a process (utils.cu:29-30, :79-82)
   std::vector<double> v0(m);
@@ -1007,22 +848,21 @@ void Solve::power_method() {
     std::normal_distribution<double> dist(0.0, 1.0);
     for (int i = 0; i < m; ++i) v0[i] = dist(gen);
   }
-  PDLP_CUDA(cudaMemcpyAsync(d.pm_v[0], v0.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st_));
-  k_pm_norm<<<d.ew_grid, kThreads, 0, st_>>>(d, d.pm_v[0]);
-  k_pm_norm_fin<<<1, kThreads, 0, st_>>>(d);
+  PDLP_CUDA(cudaMemcpyAsync(w.v[0], v0.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st_));
+  k_pm_norm<<<w.ew_grid, kThreads, 0, st_>>>(w, w.v[0]);
+  k_pm_norm_fin<<<1, kThreads, 0, st_>>>(w);
   PDLP_LAUNCH_CHECK();
+  launches_ += 2;
   // chunks of power iterations, captured once and replayed until converged
   const int CH = 16;
   auto enqueue = [&](int it) {
-    const double *v = d.pm_v[it & 1];
-    double *vn = d.pm_v[(it + 1) & 1];
-    PowAtEpi e1{d, v, 0.0};
-    launch_spmv(AT_, e1, nullptr, nullptr, st_);
-    PowAEpi e2{d, v, vn, 0.0};
-    launch_spmv(A_, e2, d.p_pa, d.lp_pa, st_);
-    k_pm_dot_fin<<<1, kThreads, 0, st_>>>(d);
-    k_pm_resid<<<d.ew_grid, kThreads, 0, st_>>>(d, v, vn);
-    k_pm_resid_fin<<<1, kThreads, 0, st_>>>(d);
+    const double *v = w.v[it & 1];
+    double *vn = w.v[(it + 1) & 1];
+    launch_spmv(AT64_, PowAtEpi{w, v, 0.0}, nullptr, nullptr, st_);
+    launch_spmv(A64_, PowAEpi{w, v, vn, 0.0}, w.p_pa, w.lp_pa, st_);
+    k_pm_dot_fin<<<1, kThreads, 0, st_>>>(w);
+    k_pm_resid<<<w.ew_grid, kThreads, 0, st_>>>(w, v, vn);
+    k_pm_resid_fin<<<1, kThreads, 0, st_>>>(w);
     PDLP_LAUNCH_CHECK();
   };
   cudaGraph_t graph;
@@ -1033,7 +873,6 @@ void Solve::power_method() {
   PDLP_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   int launched = 0;
   const int maxit = p_.sv_max_iter;
-  // the chunk runs CH iterations; the last partial chunk is run unrolled
   while (launched + CH <= maxit) {
     PDLP_CUDA(cudaGraphLaunch(exec, st_));
     launched += CH;
@@ -1042,24 +881,30 @@ void Solve::power_method() {
     if (hflag_->pm_done) break;
   }
   if (!hflag_->pm_done)
-    for (int i = launched; i < maxit; ++i) enqueue(i - launched);  // parity restarts at 0: even CH
+    for (int i = launched; i < maxit; ++i) {  // even CH: parity restarts at 0
+      enqueue(i - launched);
+      launches_ += 5;
+    }
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
   Ctl c;
-  PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
+  PDLP_CUDA(cudaMemcpyAsync(&c, w.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
   pm_iters_ = c.pm_iters;
   sigma_max_ = sqrt(c.pm_sigma_sq);
 }
 
-void Solve::init_step() {
-  Dev &d = d_;
+template <class T>
+void Solve<T>::init_step(double known_sigma, double known_omega) {
+  Dev<T> &d = d_;
   double eta = 1.0;
-  if (A_.nnz > 0 && d.m > 0) {
-    power_method();
+  if (A64_.nnz > 0 && d.m > 0) {
+    if (known_sigma > 0.0) sigma_max_ = known_sigma;
+    else power_method();
     eta = 0.998 / sigma_max_;
   }
   double omega = p_.bound_objective_rescaling ? 1.0 : (d.cnorm + 1.0) / (d.bnorm + 1.0);
+  if (known_omega > 0.0) omega = known_omega;
   // ctl offsets of step_size/primal_weight/best_primal_weight are the first 3 doubles
   double s[3] = {eta, omega, omega};
   PDLP_CUDA(cudaMemcpyAsync(d.ctl, s, sizeof(s), cudaMemcpyHostToDevice, st_));
@@ -1068,48 +913,70 @@ void Solve::init_step() {
   PDLP_CUDA(cudaStreamSynchronize(st_));
 }
 
-void Solve::enqueue_eval(int t, int off, bool infeas, bool restart_check, bool final_eval) {
-  (void)t;
-  Dev &d = d_;
+template <class T>
+void Solve<T>::enqueue_eval(int off, bool infeas, bool restart_check, int mode) {
+  Dev<T> &d = d_;
   if (d.linf) {
-    launch_spmv(A_, EvalAEpi<true>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<true>{d}, d.p_e2, d.lp_e2, st_);
+    launch_spmv(A_, EvalAEpi<T, true>{d}, d.p_e1, d.lp_e1, st_);
+    launch_spmv(AT_, EvalATEpi<T, true>{d}, d.p_e2, d.lp_e2, st_);
   } else {
-    launch_spmv(A_, EvalAEpi<false>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<false>{d}, d.p_e2, d.lp_e2, st_);
+    launch_spmv(A_, EvalAEpi<T, false>{d}, d.p_e1, d.lp_e1, st_);
+    launch_spmv(AT_, EvalATEpi<T, false>{d}, d.p_e2, d.lp_e2, st_);
   }
-  launches_ += 2;
   if (infeas) {
-    k_ray_project<<<d.ew_grid, kThreads, 0, st_>>>(d);
-    k_ray_project_fin<<<1, kThreads, 0, st_>>>(d);
-    launch_spmv(A_, InfAEpi{d, 0.0}, d.p_i1, d.lp_i1, st_);
-    launch_spmv(AT_, InfATEpi{d, 0.0}, d.p_i2, d.lp_i2, st_);
-    launches_ += 4;
+    k_ray_project<T><<<d.ew_grid, kThreads, 0, st_>>>(d);
+    k_ray_project_fin<T><<<1, kThreads, 0, st_>>>(d);
+    launch_spmv(A_, InfAEpi<T>{d, T(0)}, d.p_i1, d.lp_i1, st_);
+    launch_spmv(AT_, InfATEpi<T>{d, T(0)}, d.p_i2, d.lp_i2, st_);
   }
-  k_eval_fin<<<1, kThreads, 0, st_>>>(d, off, infeas, restart_check, final_eval);
+  k_eval_fin<T><<<1, kThreads, 0, st_>>>(d, off, infeas, restart_check, mode);
   PDLP_LAUNCH_CHECK();
-  launches_ += 1;
+  if (snapshot_ && mode == kEvalCheck) {
+    k_snapshot<T><<<d.ew_grid, kThreads, 0, st_>>>(d);
+    PDLP_LAUNCH_CHECK();
+  }
 }
 
-void Solve::enqueue_iteration(int t, int off, bool) {
-  Dev &d = d_;
+template <class T>
+void Solve<T>::enable_snapshot() {
+  if (snapshot_) return;
+  Dev<T> &d = d_;
+  size_t bytes = ((size_t)d.n * 2 + d.m) * sizeof(T) + 1024;
+  void *mem = nullptr;
+  PDLP_CUDA(cudaMalloc(&mem, bytes));
+  snap_mem_ = mem;
+  d.bx = (T *)mem;
+  d.bl = d.bx + d.n;
+  d.by = d.bl + d.n;
+  snapshot_ = true;
+}
+
+template <class T>
+double Solve<T>::primal_weight() const {
+  Ctl c;
+  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  return c.primal_weight;
+}
+
+template <class T>
+void Solve<T>::enqueue_iteration(int t, int off) {
+  Dev<T> &d = d_;
   IterFlags f = iteration_flags(t, d.F);
   const int par = t & 1;
-  double *xc = d.x[par], *xn = d.x[par ^ 1];
-  double *yc = d.y[par], *yn = d.y[par ^ 1];
-  if (f.eval) enqueue_eval(t, off, f.infeas, f.restart_check, false);
+  T *xc = d.x[par], *xn = d.x[par ^ 1];
+  T *yc = d.y[par], *yn = d.y[par ^ 1];
+  if (f.eval) enqueue_eval(off, f.infeas, f.restart_check, kEvalCheck);
   if (f.maybe_restart) {
-    k_restart<<<d.ew_grid, kThreads, 0, st_>>>(d, xc, yc);
-    k_restart_fin<<<1, kThreads, 0, st_>>>(d, off);
+    k_restart<T><<<d.ew_grid, kThreads, 0, st_>>>(d, xc, yc);
+    k_restart_fin<T><<<1, kThreads, 0, st_>>>(d, off);
     PDLP_LAUNCH_CHECK();
-    launches_ += 2;
   }
-#define PDLP_STEPS(MAJ, FP)                                                         \
-  {                                                                                 \
-    PrimalEpi<MAJ, FP> pe{d, off, xc, yc, xn, 0.0, 0.0, 0.0};                       \
-    launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                               \
-    DualEpi<MAJ, FP> de{d, off, yc, yn, 0.0, 0.0, 0.0, 0.0};                        \
-    launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                                \
+#define PDLP_STEPS(MAJ, FP)                                             \
+  {                                                                     \
+    PrimalEpi<T, MAJ, FP> pe{d, off, xc, yc, xn, T(0), T(0), T(0)};     \
+    launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                   \
+    DualEpi<T, MAJ, FP> de{d, off, yc, yn, T(0), T(0), T(0), T(0)};     \
+    launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                    \
   }
   if (f.major_kernel) {
     if (f.fpe) PDLP_STEPS(true, true) else PDLP_STEPS(true, false)
@@ -1117,19 +984,23 @@ void Solve::enqueue_iteration(int t, int off, bool) {
     if (f.fpe) PDLP_STEPS(false, true) else PDLP_STEPS(false, false)
   }
 #undef PDLP_STEPS
-  launches_ += 2;
   if (f.fpe) {
-    if (f.fpe_restart_only) launch_spmv(AT_, FpeEpi<true>{d}, d.p_fpe, d.lp_fpe, st_);
-    else launch_spmv(AT_, FpeEpi<false>{d}, d.p_fpe, d.lp_fpe, st_);
-    k_fpe_fin<<<1, kThreads, 0, st_>>>(d, f.fpe_restart_only ? 1 : 0);
+    if (f.fpe_restart_only) launch_spmv(AT_, FpeEpi<T, true>{d}, d.p_fpe, d.lp_fpe, st_);
+    else launch_spmv(AT_, FpeEpi<T, false>{d}, d.p_fpe, d.lp_fpe, st_);
+    k_fpe_fin<T><<<1, kThreads, 0, st_>>>(d, f.fpe_restart_only ? 1 : 0);
     PDLP_LAUNCH_CHECK();
-    launches_ += 2;
   }
 }
 
-cudaGraphExec_t Solve::chunk_graph(int t0, int t1) {
+// kernels one iteration launches (early exits included)
+static long iteration_launches(const IterFlags &f) {
+  return 2 + (f.eval ? 3 + (f.infeas ? 4 : 0) : 0) + (f.maybe_restart ? 2 : 0) + (f.fpe ? 2 : 0);
+}
+
+template <class T>
+cudaGraphExec_t Solve<T>::chunk_graph(int t0, int t1) {
   std::string key;
-  key.reserve((size_t)(t1 - t0) * 8 + 8);
+  key.reserve((size_t)(t1 - t0) * 2 + 2);
   key += (char)('0' + (t0 & 1));
   for (int t = t0; t < t1; ++t) {
     IterFlags f = iteration_flags(t, d_.F);
@@ -1140,24 +1011,24 @@ cudaGraphExec_t Solve::chunk_graph(int t0, int t1) {
   if (it != graphs_.end()) return it->second;
   cudaGraph_t g;
   cudaGraphExec_t e;
-  long saved = launches_;
   PDLP_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-  for (int t = t0; t < t1; ++t) enqueue_iteration(t, t - t0, true);
+  for (int t = t0; t < t1; ++t) enqueue_iteration(t, t - t0);
   PDLP_CUDA(cudaStreamEndCapture(st_, &g));
   PDLP_CUDA(cudaGraphInstantiate(&e, g, 0));
-  launches_ = saved;
   raw_graphs_.push_back(g);
   graphs_[key] = e;
   return e;
 }
 
-void Solve::run() {
-  Dev &d = d_;
+template <class T>
+void Solve<T>::run() {
+  Dev<T> &d = d_;
   const int L = p_.termination_criteria.iteration_limit;
   const int CH = 100;
   auto t0 = std::chrono::steady_clock::now();
   k_loop_start<<<1, 1, 0, st_>>>(d.ctl);
   PDLP_LAUNCH_CHECK();
+  launches_ += 1;
   cudaEvent_t ev[2];
   PDLP_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
   PDLP_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
@@ -1172,12 +1043,7 @@ void Solve::run() {
     PDLP_LAUNCH_CHECK();
     PDLP_CUDA(cudaGraphLaunch(g, st_));
     PDLP_CUDA(cudaEventRecord(ev[k & 1], st_));
-    // count kernels of the chunk (device-side early exits still launch)
-    for (int tt = t; tt < t1; ++tt) {
-      IterFlags f = iteration_flags(tt, d.F);
-      launches_ += 2 + (f.eval ? 3 + (f.infeas ? 4 : 0) : 0) + (f.maybe_restart ? 2 : 0) +
-                   (f.fpe ? 2 : 0);
-    }
+    for (int tt = t; tt < t1; ++tt) launches_ += iteration_launches(iteration_flags(tt, d.F));
     launches_ += 1;
     ++k;
     t = t1;
@@ -1188,14 +1054,16 @@ void Solve::run() {
   if (!hflag_->done) {
     // iteration limit: one more evaluation at total_count = L (solver.cu:105-109)
     k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, L);
-    enqueue_eval(L, 0, false, false, true);
+    enqueue_eval(0, false, false, kEvalIterLimit);
+    launches_ += 4;
     PDLP_CUDA(cudaStreamSynchronize(st_));
   }
   loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void Solve::time_kernels(int reps, double *ms) {
-  Dev &d = d_;
+template <class T>
+void Solve<T>::time_kernels(int reps, double *ms) {
+  Dev<T> &d = d_;
   cudaEvent_t e0, e1;
   PDLP_CUDA(cudaEventCreate(&e0));
   PDLP_CUDA(cudaEventCreate(&e1));
@@ -1209,17 +1077,32 @@ void Solve::time_kernels(int reps, double *ms) {
     PDLP_CUDA(cudaEventElapsedTime(&t, e0, e1));
     return (double)t / reps;
   };
-  PrimalEpi<false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], 0.0, 0.0, 0.0};
-  DualEpi<false, false> de{d, 0, d.y[0], d.y[1], 0.0, 0.0, 0.0, 0.0};
+  PrimalEpi<T, false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
+  DualEpi<T, false, false> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
   ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
   ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
-  ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<false>{d}, d.p_e1, d.lp_e1, st_); });
-  ms[3] = timed([&] { launch_spmv(AT_, EvalATEpi<false>{d}, d.p_e2, d.lp_e2, st_); });
+  ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<T, false>{d}, d.p_e1, d.lp_e1, st_); });
+  ms[3] = timed([&] { launch_spmv(AT_, EvalATEpi<T, false>{d}, d.p_e2, d.lp_e2, st_); });
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
 }
 
-std::vector<double> Solve::trace() const {
+template <class T>
+int Solve<T>::reason() const {
+  Ctl c;
+  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  return c.reason;
+}
+
+template <class T>
+int Solve<T>::total_count() const {
+  Ctl c;
+  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  return c.final_t;
+}
+
+template <class T>
+std::vector<double> Solve<T>::trace() const {
   Ctl c;
   PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   std::vector<double> tr((size_t)c.trace_len * 10);
@@ -1228,12 +1111,44 @@ std::vector<double> Solve::trace() const {
   return tr;
 }
 
-cupdlpx_result_t *Solve::result() {
-  Dev &d = d_;
-  const int n = d.n, m = d.m;
-  launch_spmv(AT_, ReducedCostEpi{d}, nullptr, nullptr, st_);
-  k_unscale<<<grid_for((long)n + m), kThreads, 0, st_>>>(d);
+template <class T>
+void Solve<T>::result_device(double *x, double *y, double *lam) {
+  Dev<T> d = d_;
+  if (snapshot_) {  // the best evaluated iterate of the run
+    Ctl c;
+    PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaStreamSynchronize(st_));
+    if (c.snap_err < INFINITY) {
+      d.xhat = d.bx;
+      d.yhat = d.by;
+      d.lam = d.bl;
+    }
+  }
+  k_unscale<T><<<grid_for((long)d.n + d.m), kThreads, 0, st_>>>(d, x, y, lam);
   PDLP_LAUNCH_CHECK();
+}
+
+template <class T>
+Kkt Solve<T>::evaluate(const double *x, const double *y, const double *lam) {
+  Dev<T> &d = d_;
+  k_scale_point<T><<<grid_for((long)d.n + d.m), kThreads, 0, st_>>>(d, x, y, lam);
+  PDLP_LAUNCH_CHECK();
+  k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, 0);
+  enqueue_eval(0, false, false, kEvalOnly);
+  Ctl c;
+  PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
+  PDLP_CUDA(cudaStreamSynchronize(st_));
+  return Kkt{c.abs_primal_res, c.rel_primal_res, c.abs_dual_res, c.rel_dual_res,
+             c.primal_obj,     c.dual_obj,       c.gap,          c.rel_gap};
+}
+
+template <class T>
+cupdlpx_result_t *Solve<T>::result() {
+  Dev<T> &d = d_;
+  const int n = d.n, m = d.m;
+  launch_spmv(AT_, ReducedCostEpi<T>{d, outl_}, nullptr, nullptr, st_);
+  result_device(outx_, outy_, nullptr);
+  launches_ += 2;
   auto *r = (cupdlpx_result_t *)calloc(1, sizeof(cupdlpx_result_t));
   if (!r) throw std::bad_alloc();
   r->primal_solution = (double *)malloc(sizeof(double) * (n ? n : 1));
@@ -1247,11 +1162,11 @@ cupdlpx_result_t *Solve::result() {
     throw std::bad_alloc();
   }
   if (n) {
-    PDLP_CUDA(cudaMemcpyAsync(r->primal_solution, d.xhat, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
-    PDLP_CUDA(cudaMemcpyAsync(r->reduced_cost, d.auxn, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaMemcpyAsync(r->primal_solution, outx_, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaMemcpyAsync(r->reduced_cost, outl_, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
   }
   if (m)
-    PDLP_CUDA(cudaMemcpyAsync(r->dual_solution, d.yhat, (size_t)m * 8, cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaMemcpyAsync(r->dual_solution, outy_, (size_t)m * 8, cudaMemcpyDeviceToHost, st_));
   Ctl c;
   PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
@@ -1283,5 +1198,8 @@ cupdlpx_result_t *Solve::result() {
   r->feasibility_iteration = 0;
   return r;
 }
+
+template class Solve<double>;
+template class Solve<float>;
 
 }  // namespace pdlp

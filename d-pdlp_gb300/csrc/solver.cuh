@@ -1,4 +1,10 @@
 // solver.cuh -- device-side data of one PDHG solve and the host driver class.
+//
+// The iteration is templated on T, the type of the matrix values, iterates
+// and per-element arithmetic: double for the FP64 path, float for the FP32
+// path.  In both, every reduction (KKT, fixed-point error, restart distances,
+// power method), every scalar of the control block, the rescaling and the
+// unscaling run in FP64.
 #pragma once
 
 #include <map>
@@ -12,25 +18,28 @@
 
 namespace pdlp {
 
-// A sparse matrix resident in HBM (CSR, int32 indices, FP64 values).
-struct DevCsr {
+// A sparse matrix resident in HBM (CSR, int32 indices, values of type T).
+template <class T>
+struct DevCsrT {
   int rows = 0, cols = 0, nnz = 0;
   int *ptr = nullptr, *col = nullptr;
-  double *val = nullptr;
+  T *val = nullptr;
   SpmvPlan plan;
 };
+using DevCsr = DevCsrT<double>;
 
 // Everything a kernel of the iteration needs, passed by value (kernel
 // parameter space), so concurrent solves never share a global.
+template <class T>
 struct Dev {
   int n, m;
   // scaled problem (reference rescale_info_t / solver state)
-  const double *c, *lv, *uv, *lc, *uc;
-  const double *lvf, *uvf, *lcf, *ucf;  // bound with +-inf replaced by 0
-  const double *Dr, *Dc;                // cumulative row / column scaling
+  const T *c, *lv, *uv, *lc, *uc;
+  const T *lvf, *uvf, *lcf, *ucf;  // bounds with +-inf replaced by 0
+  const double *Dr, *Dc;           // cumulative row / column scaling (FP64)
   // iterates
-  double *x[2], *x0, *xref, *xhat, *lam, *dx, *auxn;
-  double *y[2], *y0, *yhat, *dy, *auxm;
+  T *x[2], *x0, *xref, *xhat, *lam, *dx, *auxn;
+  T *y[2], *y0, *yhat, *dy, *auxm;
   Ctl *ctl;
   HostFlag *hflag;  // mapped pinned host memory
   double *trace;
@@ -41,7 +50,19 @@ struct Dev {
   int F, linf, verbose;
   double eps_opt, eps_feas, eps_inf, time_limit;
   double art, suff, nec, kp, ki, kd, ismooth;
-  double sv_tol;
+  // stall rule (FP32 rounds of the refinement): stop when the KKT error has
+  // not improved by 10% within max(stall_min, stall_frac * t) iterations;
+  // stall_min = 0 disables it
+  int stall_min;
+  double stall_frac;
+  // shifted evaluation (refinement rounds): the solve works on a correction
+  // LP centred at (sx, sy); the objectives are then those of the original
+  // LP at (sx + x, sy + y), from its objective and finite bounds
+  int shifted;
+  const double *sx, *sy, *oc, *olcf, *oucf;
+  double oc0;
+  // best-iterate snapshot (refinement rounds): copies of x_hat, y_hat, lam
+  T *bx, *by, *bl;
   // reduction partials, one buffer per launch site
   int nblkA, nlongA, nblkT, nlongT, ew_grid;
   double *p_pstep, *lp_pstep;  // primal step: sum dx^2
@@ -53,13 +74,25 @@ struct Dev {
   double *p_i1, *lp_i1;        // ray over A (2)
   double *p_i2, *lp_i2;        // ray over A^T (3)
   double *p_rs;                // restart distances (2 x ew_grid)
-  double *p_pa, *lp_pa;        // power A (2)
-  double *p_pr;                // power residual / norm (1 x ew_grid)
-  double *pm_v[2], *pm_g;      // power vectors (m, m, n)
   double *p_misc;              // kMiscPart doubles for set-up reductions
 };
 
+// The power method always runs in FP64 on the FP64 scaled matrix.
+struct PowDev {
+  int n, m;
+  Ctl *ctl;
+  HostFlag *hflag;
+  double *v[2], *g;
+  double *p_pa, *lp_pa, *p_pr;
+  int nblkA, nlongA, ew_grid;
+  double sv_tol;
+};
+
 constexpr int kMiscPart = 4096;
+
+// Termination reason of an FP32 refinement round that stopped improving;
+// internal, never returned to callers.
+constexpr int kReasonStalled = 100;
 
 // Host flags describing one iteration of the reference driver loop
 // (reference src/solver.cu:58-103).
@@ -83,14 +116,20 @@ inline IterFlags iteration_flags(int t, int F) {
 
 // An LP resident in HBM, as the caller gave it (unscaled): A and its
 // transpose in CSR with their SpMV plans, bounds, objective, warm start.
-// Read-only once built; any number of solves can run from it.
+// Read-only once built; any number of solves can run from it.  A derived
+// problem (refinement) shares the matrices of its parent and owns only its
+// vectors.
 struct DevProblem {
   int m = 0, n = 0, nnz = 0, tile = 0;
   DevCsr A, AT;  // original values; plan scratch (lcnt/lsum) is per solve
   double *c = nullptr, *lv = nullptr, *uv = nullptr, *lc = nullptr, *uc = nullptr;
   double *xs = nullptr, *ys = nullptr;  // warm start (unscaled) or null
   double cnorm_l2 = 0, cnorm_linf = 0, bnorm_l2 = 0, bnorm_linf = 0, c0 = 0;
-  void *arena = nullptr;
+  // correction LP of a refinement round: centre and original objective data
+  const double *shift_x = nullptr, *shift_y = nullptr, *orig_c = nullptr;
+  const double *orig_lcf = nullptr, *orig_ucf = nullptr;
+  double orig_c0 = 0;
+  void *arena = nullptr;  // owned device memory (null for a view)
   size_t bytes = 0;
   ~DevProblem();
 };
@@ -98,21 +137,45 @@ struct DevProblem {
 // Validate, transpose (host), plan and upload.  Throws on a malformed CSR.
 DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st);
 
-// One single-LP FP64 solve on one stream.
+// KKT measures of a point, in the reference's definitions.
+struct Kkt {
+  double abs_p, rel_p, abs_d, rel_d, pobj, dobj, gap, rel_gap;
+};
+
+// One single-LP solve on one stream; T = double (FP64 path) or float (FP32
+// path with FP64 reductions).
+template <class T>
 class Solve {
  public:
   Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
         int trace_cap = 0);
+  // Enable the stall rule (before run()).
+  void set_stall_rule(int min_iters, double frac) {
+    d_.stall_min = min_iters;
+    d_.stall_frac = frac;
+  }
   ~Solve();
   // Working copy of the problem, GPU rescaling, finite bounds, warm start.
   void prepare();
-  // Power method -> step size; initial primal weight.
-  void init_step();
+  // Power method -> step size (skipped when known_sigma > 0); initial primal
+  // weight (known_omega > 0 overrides the reference's choice).
+  void init_step(double known_sigma = 0.0, double known_omega = 0.0);
+  // Keep the best-KKT iterate of the run (refinement rounds); result_device
+  // then returns it.  Call before run().
+  void enable_snapshot();
+  // scalings and final primal weight (after prepare / run)
+  double cb() const { return d_.cb; }
+  double ob() const { return d_.ob; }
+  double primal_weight() const;
   // Main loop until termination or iteration limit.
   void run();
   // Reduced cost, unscale, copy to a malloc'ed result.
   cupdlpx_result_t *result();
-
+  // Unscaled FP64 primal, dual and dual slack into device buffers.
+  void result_device(double *x, double *y, double *lam);
+  // KKT of the given unscaled point (device buffers) on this solve's problem;
+  // meaningful for a solve prepared without rescaling.
+  Kkt evaluate(const double *x, const double *y, const double *lam);
   // Average device time (ms) of the plain-iteration kernels, measured with
   // CUDA events on the solve's stream over `reps` launches each:
   // ms[0] primal step (A^T SpMV + update), ms[1] dual step (A SpMV + update),
@@ -127,22 +190,36 @@ class Solve {
   double loop_seconds() const { return loop_sec_; }
   int graph_count() const { return (int)graphs_.size(); }
   long kernel_launches() const { return launches_; }
-  const Dev &dev() const { return d_; }
-  const DevCsr &A() const { return A_; }
-  const DevCsr &AT() const { return AT_; }
+  // termination reason and iteration count after run()
+  int reason() const;
+  int total_count() const;
+  const Dev<T> &dev() const { return d_; }
+  const DevCsrT<T> &A() const { return A_; }
+  const DevCsr &A64() const { return A64_; }
+  // scaled FP64 vectors (valid after prepare)
+  const double *c64() const { return c64_; }
+  const double *lv64() const { return lv64_; }
+  const double *uv64() const { return uv64_; }
+  const double *lc64() const { return lc64_; }
+  const double *uc64() const { return uc64_; }
 
  private:
   void alloc();
-  void enqueue_iteration(int t, int off, bool capture);
-  void enqueue_eval(int t, int off, bool infeas, bool restart_check, bool final_eval);
+  void enqueue_iteration(int t, int off);
+  void enqueue_eval(int off, bool infeas, bool restart_check, int mode);
   cudaGraphExec_t chunk_graph(int t0, int t1);
   void power_method();
 
   pdhg_parameters_t p_;
   cudaStream_t st_;
   const DevProblem &P_;
-  Dev d_{};
-  DevCsr A_, AT_;
+  Dev<T> d_{};
+  PowDev pw_{};
+  DevCsr A64_, AT64_;   // FP64 scaled working copies (rescaling, power method)
+  DevCsrT<T> A_, AT_;   // iteration matrices (== A64_/AT64_ for T = double)
+  double *c64_ = nullptr, *lv64_ = nullptr, *uv64_ = nullptr, *lc64_ = nullptr,
+         *uc64_ = nullptr;
+  double *outx_ = nullptr, *outy_ = nullptr, *outl_ = nullptr;  // FP64 results
   void *arena_ = nullptr;
   HostFlag *hflag_ = nullptr;
   int trace_cap_ = 0;
@@ -152,7 +229,8 @@ class Solve {
   double sigma_max_ = 0.0;
   double rescale_sec_ = 0.0, loop_sec_ = 0.0;
   long launches_ = 0;
-  bool counting_ = true;
+  bool snapshot_ = false;
+  void *snap_mem_ = nullptr;
 };
 
 // GPU rescaling (precond.cu): Ruiz, Pock-Chambolle, bound/objective scaling
@@ -166,5 +244,27 @@ void gpu_rescale(const pdhg_parameters_t &p, DevCsr &A, DevCsr &AT, double *c,
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
                     std::vector<int> &tp, std::vector<int> &tj,
                     std::vector<double> &tx);
+
+// Options of the mixed-precision solve (refine.cu).
+struct RefineOptions {
+  int max_rounds = 8;       // outer refinement rounds
+  double inner_eps = 0.0;   // tolerance of each FP32 solve (0: automatic)
+};
+
+struct RefineReport {
+  int rounds = 0;
+  int power_iterations = 0;
+  double sigma_max = 0.0;
+  long inner_iterations = 0;
+  long kernel_launches = 0;
+  double seconds = 0.0;
+  Kkt kkt{};
+};
+
+// FP32 PDHG with FP64 iterative refinement on a resident problem; returns
+// a result in the layout of solve_lp_problem.
+cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &params,
+                                const RefineOptions &opt, cudaStream_t st,
+                                RefineReport *report);
 
 }  // namespace pdlp

@@ -173,7 +173,16 @@ class SolveInfo(C.Structure):
         ("graphs", C.c_int),
         ("kernel_launches", C.c_longlong),
         ("device_seconds", C.c_double),
+        ("refinement_rounds", C.c_int),
+        ("precision", C.c_int),
     ]
+
+
+PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("max_refinements", C.c_int), ("inner_eps", C.c_double)]
 
 
 # -------------------------------------------------------------- prototypes
@@ -225,6 +234,15 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_device_problem_solve.restype = R
     lib.pdlp_device_problem_solve.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                               C.POINTER(SolveInfo)]
+    lib.pdlp_solve_opts.restype = R
+    lib.pdlp_solve_opts.argtypes = [P, C.POINTER(PdhgParameters), C.POINTER(Options),
+                                    C.POINTER(SolveInfo)]
+    lib.pdlp_device_problem_solve_opts.restype = R
+    lib.pdlp_device_problem_solve_opts.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
+                                                   C.POINTER(Options), C.POINTER(SolveInfo)]
+    lib.pdlp_device_problem_time_kernels_prec.restype = C.c_int
+    lib.pdlp_device_problem_time_kernels_prec.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
+                                                          C.c_int, C.c_int, _dp]
     lib.pdlp_device_problem_time_kernels.restype = C.c_int
     lib.pdlp_device_problem_time_kernels.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                                      C.c_int, _dp]
@@ -367,10 +385,31 @@ class SolveOutput:
     info: dict = field(default_factory=dict)
 
 
+def make_options(precision: int = 0, max_refinements: int = 0, inner_eps: float = 0.0) -> Options:
+    o = Options()
+    o.precision, o.max_refinements, o.inner_eps = precision, max_refinements, inner_eps
+    return o
+
+
 def solve(problem: Problem, params: PdhgParameters | None = None, trace_cap: int = 0,
-          library: C.CDLL | None = None) -> SolveOutput:
-    """Solve through pdlp_solve_ex; raises on failure."""
+          library: C.CDLL | None = None, precision: int = PRECISION_FP64,
+          max_refinements: int = 0) -> SolveOutput:
+    """Solve through pdlp_solve_ex (FP64) or pdlp_solve_opts (FP32 +
+    refinement); raises on failure."""
     L = library or lib()
+    if precision != PRECISION_FP64:
+        info = SolveInfo()
+        o = make_options(precision, max_refinements)
+        pp = C.byref(params) if params is not None else None
+        r = L.pdlp_solve_opts(problem.ptr, pp, C.byref(o), C.byref(info))
+        if not r:
+            raise RuntimeError("solve failed: " + L.pdlp_last_error().decode())
+        try:
+            res = result_dict(r)
+        finally:
+            L.cupdlpx_result_free(r)
+        return SolveOutput(res, np.zeros((0, TRACE_WIDTH)),
+                           {f: getattr(info, f) for f, _ in SolveInfo._fields_})
     tr = np.zeros((max(trace_cap, 1), TRACE_WIDTH))
     tl = C.c_int(0)
     info = SolveInfo()
@@ -400,10 +439,12 @@ class DeviceProblem:
     def nbytes(self) -> int:
         return self._lib.pdlp_device_problem_bytes(self.handle)
 
-    def solve(self, params: PdhgParameters | None = None) -> SolveOutput:
+    def solve(self, params: PdhgParameters | None = None, precision: int = PRECISION_FP64,
+              max_refinements: int = 0) -> SolveOutput:
         info = SolveInfo()
         pp = C.byref(params) if params is not None else None
-        r = self._lib.pdlp_device_problem_solve(self.handle, pp, C.byref(info))
+        o = make_options(precision, max_refinements)
+        r = self._lib.pdlp_device_problem_solve_opts(self.handle, pp, C.byref(o), C.byref(info))
         if not r:
             raise RuntimeError("solve failed: " + self._lib.pdlp_last_error().decode())
         try:
@@ -413,10 +454,12 @@ class DeviceProblem:
         return SolveOutput(res, np.zeros((0, TRACE_WIDTH)),
                            {f: getattr(info, f) for f, _ in SolveInfo._fields_})
 
-    def time_kernels(self, params: PdhgParameters | None = None, reps: int = 20) -> np.ndarray:
+    def time_kernels(self, params: PdhgParameters | None = None, reps: int = 20,
+                     precision: int = PRECISION_FP64) -> np.ndarray:
         ms = np.zeros(4)
         pp = C.byref(params) if params is not None else None
-        if self._lib.pdlp_device_problem_time_kernels(self.handle, pp, reps, as_dp(ms)) != 0:
+        if self._lib.pdlp_device_problem_time_kernels_prec(self.handle, pp, precision, reps,
+                                                           as_dp(ms)) != 0:
             raise RuntimeError("kernel timing failed: " + self._lib.pdlp_last_error().decode())
         return ms
 

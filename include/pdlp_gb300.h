@@ -29,7 +29,34 @@ typedef struct {
   long long kernel_launches;  /* kernels launched by the solve */
   double device_seconds;      /* CUDA events on the solve's stream, from the
                                  first copy/kernel to the result on the host */
+  int refinement_rounds;      /* FP32 rounds of a mixed-precision solve */
+  int precision;              /* PDLP_PRECISION_* the solve ran in */
 } pdlp_solve_info_t;
+
+/* Arithmetic of the PDHG iteration.
+ * FP64: every operation in FP64, as the reference.
+ * FP32_REFINE: matrix values, iterates, SpMVs and updates in FP32 (FP32
+ *   accumulation); KKT / gap / restart / primal-weight reductions, objective
+ *   values and the refinement residuals in FP64.  Rounds of iterative
+ *   refinement re-centre the LP at the FP64 point until the FP64 KKT of the
+ *   original problem meets the requested tolerances.
+ * The drop-in solve_lp_problem() uses FP64 unless the environment variable
+ * PDLP_PRECISION is "fp32". */
+#define PDLP_PRECISION_FP64 0
+#define PDLP_PRECISION_FP32_REFINE 1
+
+typedef struct {
+  int precision;          /* PDLP_PRECISION_* */
+  int max_refinements;    /* FP32 rounds (0: 8) */
+  double inner_eps;       /* tolerance of rounds after the first (0: the
+                             requested tolerances) */
+} pdlp_options_t;
+
+/* solve_lp_problem with explicit options (NULL: FP64). */
+cupdlpx_result_t *pdlp_solve_opts(const lp_problem_t *prob,
+                                  const pdhg_parameters_t *params,
+                                  const pdlp_options_t *opts,
+                                  pdlp_solve_info_t *info);
 
 /* Number of doubles per trace record written by pdlp_solve_ex: iteration,
  * rel. primal residual, rel. dual residual, rel. gap, primal objective,
@@ -59,6 +86,11 @@ long long pdlp_device_problem_bytes(const pdlp_device_problem_t *dp);
 cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
                                             const pdhg_parameters_t *params,
                                             pdlp_solve_info_t *info);
+/* pdlp_device_problem_solve with explicit options (NULL: FP64). */
+cupdlpx_result_t *pdlp_device_problem_solve_opts(pdlp_device_problem_t *dp,
+                                                 const pdhg_parameters_t *params,
+                                                 const pdlp_options_t *opts,
+                                                 pdlp_solve_info_t *info);
 /* Average device milliseconds per launch of the iteration kernels, timed
  * with CUDA events on the solve's stream over `reps` launches each:
  * ms[0] primal step (A^T SpMV + projection + Halpern), ms[1] dual step
@@ -67,6 +99,10 @@ cupdlpx_result_t *pdlp_device_problem_solve(pdlp_device_problem_t *dp,
 int pdlp_device_problem_time_kernels(pdlp_device_problem_t *dp,
                                      const pdhg_parameters_t *params, int reps,
                                      double *ms);
+/* As above for the given PDLP_PRECISION_* iteration type. */
+int pdlp_device_problem_time_kernels_prec(pdlp_device_problem_t *dp,
+                                          const pdhg_parameters_t *params,
+                                          int precision, int reps, double *ms);
 
 /* Message of the last failure in this thread ("" if none). */
 const char *pdlp_last_error(void);
