@@ -206,7 +206,8 @@ def run_ours(args, cp, rank, world, local):
     a = prob.arrays()
     m, n, nnz = a["m"], a["n"], a["nnz"]
     params = params_for(cp, args.eps)
-    prec = cp.PRECISION_FP32_REFINE if args.precision == "fp32" else cp.PRECISION_FP64
+    prec = {"fp32": cp.PRECISION_FP32_REFINE, "fp32m": cp.PRECISION_FP32_MATRIX,
+            "fp64": cp.PRECISION_FP64}[args.precision]
     dp = cp.DeviceProblem(prob)
     for _ in range(args.warmup):
         out = dp.solve(params, precision=prec)
@@ -256,7 +257,12 @@ def run_ours(args, cp, rank, world, local):
         e2e_mean = statistics.mean(e2e_s)
     r = last.result
     ms = dp.time_kernels(params, reps=args.kernel_reps, precision=prec)
-    pb, db = kernel_bytes(m, n, nnz, 4 if prec != cp.PRECISION_FP64 else 8)
+    pb, db = kernel_bytes(m, n, nnz, 8)
+    if prec == cp.PRECISION_FP32_REFINE:
+        pb, db = kernel_bytes(m, n, nnz, 4)
+    elif prec == cp.PRECISION_FP32_MATRIX:  # 4-byte values, 8-byte vectors
+        pb -= 4 * nnz
+        db -= 4 * nnz
     kernels = {"primal_step": (ms[0], pb), "dual_step": (ms[1], db)}
     dom = max(kernels, key=lambda k: kernels[k][0])
     peak, peak_kind = load_peaks()
@@ -269,13 +275,18 @@ def run_ours(args, cp, rank, world, local):
         "metric": METRIC, "value": round(value, 4), "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1e3, 2),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 iterates + f64 KKT/refinement" if prec != cp.PRECISION_FP64 else "f64",
+        "dtype": {cp.PRECISION_FP32_REFINE: "f32 iterates + f64 KKT/refinement",
+                  cp.PRECISION_FP32_MATRIX: "f32 matrix/SpMV + f64 iterates/KKT/refinement",
+                  cp.PRECISION_FP64: "f64"}[prec],
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": name, "description": WORKLOADS[name]["desc"], "m": m, "n": n,
                    "nnz": nnz, "eps": args.eps,
-                   "precision": ("FP32 PDHG + FP64 iterative refinement (FP64 KKT of the "
-                                 "original LP meets eps)") if prec != cp.PRECISION_FP64
-                   else "FP64 plain PDHG",
+                   "precision": {
+                       cp.PRECISION_FP32_REFINE: "FP32 PDHG + FP64 iterative refinement",
+                       cp.PRECISION_FP32_MATRIX: "FP32 matrix and SpMVs (FP32 accumulation), "
+                                                 "FP64 iterates + FP64 iterative refinement",
+                       cp.PRECISION_FP64: "FP64 plain PDHG"}[prec]
+                   + " (termination: FP64 KKT of the original LP meets eps)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs (A and A^T, 480 MB) larger than L2; no flush needed"},
         "e2e": {"value": round(e2e_mean, 4), "unit": "s", "h2d_bytes_per_step": h2d,
@@ -358,8 +369,9 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-4)
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32",
-                    help="fp32: FP32 iterates + FP64 refinement (default); fp64: plain FP64")
+    ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default="fp32m",
+                    help="fp32: FP32 iterates + FP64 refinement; fp32m (default): FP32 matrix "
+                         "and SpMVs with FP64 iterates + FP64 refinement; fp64: plain FP64")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed FP64 solves reported beside an FP32 run (0: skip)")
     args = ap.parse_args()

@@ -289,6 +289,7 @@ cupdlpx_result_t *run_refined(const pdlp::DevProblem &P, const pdhg_parameters_t
   pdlp::RefineOptions ro;
   if (o.max_refinements > 0) ro.max_rounds = o.max_refinements;
   ro.inner_eps = o.inner_eps;
+  ro.fp64_iterates = o.precision == PDLP_PRECISION_FP32_MATRIX;
   pdlp::RefineReport rep;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   PDLP_CUDA(cudaEventCreate(&ev0));
@@ -310,7 +311,7 @@ cupdlpx_result_t *run_refined(const pdlp::DevProblem &P, const pdhg_parameters_t
     info->refinement_rounds = rep.rounds;
     info->power_iterations = rep.power_iterations;
     info->sigma_max = rep.sigma_max;
-    info->precision = PDLP_PRECISION_FP32_REFINE;
+    info->precision = o.precision;
   }
   return r;
 }
@@ -321,6 +322,8 @@ pdlp_options_t env_options() {
   const char *e = getenv("PDLP_PRECISION");
   if (e && (strcmp(e, "fp32") == 0 || strcmp(e, "FP32") == 0))
     o.precision = PDLP_PRECISION_FP32_REFINE;
+  if (e && (strcmp(e, "fp32m") == 0 || strcmp(e, "FP32M") == 0))
+    o.precision = PDLP_PRECISION_FP32_MATRIX;
   return o;
 }
 
@@ -356,7 +359,7 @@ cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *
     std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(prob, sg.s));
     pdlp_options_t o = opts ? *opts : env_options();
     cupdlpx_result_t *r =
-        o.precision == PDLP_PRECISION_FP32_REFINE
+        o.precision != PDLP_PRECISION_FP64
             ? run_refined(*P, p, o, sg.s, info, t0)
             : run_solve(*P, p, sg.s, trace, trace_cap, trace_len, info, t0);
     if (!quiet_summary()) final_log(r, &p);
@@ -645,7 +648,7 @@ cupdlpx_result_t *pdlp_device_problem_solve_opts(pdlp_device_problem_t *dp,
     pdlp_options_t o;
     memset(&o, 0, sizeof(o));
     if (opts) o = *opts;
-    cupdlpx_result_t *r = o.precision == PDLP_PRECISION_FP32_REFINE
+    cupdlpx_result_t *r = o.precision != PDLP_PRECISION_FP64
                               ? run_refined(*dp->P, p, o, sg.s, info, t0)
                               : run_solve(*dp->P, p, sg.s, nullptr, 0, nullptr, info, t0);
     if (!quiet_summary()) final_log(r, &p);
@@ -670,7 +673,12 @@ int pdlp_device_problem_time_kernels_prec(pdlp_device_problem_t *dp,
   if (!prepare_params(params, p)) return -1;
   try {
     StreamGuard sg;
-    if (precision == PDLP_PRECISION_FP32_REFINE) {
+    if (precision == PDLP_PRECISION_FP32_MATRIX) {
+      pdlp::Solve<double, float> s(p, sg.s, *dp->P, 0);
+      s.prepare();
+      s.init_step();
+      s.time_kernels(reps, ms);
+    } else if (precision == PDLP_PRECISION_FP32_REFINE) {
       pdlp::Solve<float> s(p, sg.s, *dp->P, 0);
       s.prepare();
       s.init_step();

@@ -29,10 +29,10 @@ __device__ __forceinline__ void halpern_weight(const Ctl *c, int off, double *sc
 
 // primal step: x_hat = proj(x - tau (c - A^T y)), x_ref = 2 x_hat - x, Halpern
 // (reference pdlp_core_op.cu:393-418, :445-462, :495-526)
-template <class T, bool MAJOR, bool FPE>
+template <class T, class M, bool MAJOR, bool FPE>
 struct PrimalEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = FPE ? 1 : 0;
   static constexpr unsigned MAXMASK = 0;
   Dev<T> d;
@@ -51,8 +51,9 @@ struct PrimalEpi {
     w = (T)sc[0];
     omw = (T)sc[1];
   }
-  __device__ T gather(int i) const { return ycur[i]; }
-  __device__ void row(int j, T s, double *acc) const {
+  __device__ M gather(int i) const { return (M)ycur[i]; }
+  __device__ void row(int j, M sm, double *acc) const {
+    T s = (T)sm;
     T xc = xcur[j];
     T t = xc - tau * (d.c[j] - s);
     T xh = fmax(d.lv[j], fmin(t, d.uv[j]));
@@ -74,10 +75,10 @@ struct PrimalEpi {
 
 // dual step: t = y/sigma - A x_ref, y_hat = sigma (t - proj(t)), Halpern
 // (reference pdlp_core_op.cu:420-443, :528-557)
-template <class T, bool MAJOR, bool FPE>
+template <class T, class M, bool MAJOR, bool FPE>
 struct DualEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = FPE ? 1 : 0;
   static constexpr unsigned MAXMASK = 0;
   Dev<T> d;
@@ -97,8 +98,9 @@ struct DualEpi {
     w = (T)sc[0];
     omw = (T)sc[1];
   }
-  __device__ T gather(int j) const { return d.xref[j]; }
-  __device__ void row(int i, T s, double *acc) const {
+  __device__ M gather(int j) const { return (M)d.xref[j]; }
+  __device__ void row(int i, M sm, double *acc) const {
+    T s = (T)sm;
     T yc = ycur[i];
     // the reference divides by sigma; one reciprocal per launch instead
     // (at most 1 ulp apart; an FP64 division costs ~10 FP64 issue slots)
@@ -118,10 +120,10 @@ struct DualEpi {
 };
 
 // cross term <A^T dy, dx> of the fixed-point error (pdlp_core_op.cu:658-696)
-template <class T, bool RESTART_ONLY>
+template <class T, class M, bool RESTART_ONLY>
 struct FpeEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 1;
   static constexpr unsigned MAXMASK = 0;
   Dev<T> d;
@@ -131,28 +133,28 @@ struct FpeEpi {
     if (RESTART_ONLY && !d.ctl->do_restart) return false;
     return true;
   }
-  __device__ T gather(int i) const { return d.dy[i]; }
-  __device__ void row(int j, T s, double *acc) const { acc[0] += (double)s * (double)d.dx[j]; }
+  __device__ M gather(int i) const { return (M)d.dy[i]; }
+  __device__ void row(int j, M s, double *acc) const { acc[0] += (double)s * (double)d.dx[j]; }
 };
 
 // KKT over A x_hat (utils.cu:503-531 constraint half), FP64 terms
-template <class T, bool LINF>
+template <class T, class M, bool LINF>
 struct EvalAEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 2;
   static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
   Dev<T> d;
   PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return !d.ctl->done; }
-  __device__ T gather(int j) const { return d.xhat[j]; }
-  __device__ void row(int i, T s, double *acc) const {
+  __device__ M gather(int j) const { return (M)d.xhat[j]; }
+  __device__ void row(int i, M s, double *acc) const {
     double sd = s;
     double cl = fmax((double)d.lc[i], fmin(sd, (double)d.uc[i]));
     double pr = (sd - cl) * d.Dr[i];
     acc[0] = LINF ? fmax(acc[0], fabs(pr)) : acc[0] + pr * pr;
     if (d.shifted) {  // original-units dual at the centre plus the correction
-      double yo = d.sy[i] + (double)d.yhat[i] / (d.Dr[i] * d.ob);
+      double yo = d.sy[i] + (double)d.yhat[i] / (d.Dr[i] * d.ob) * d.sdd_inv;
       acc[1] += fmax(yo, 0.0) * d.olcf[i] + fmin(yo, 0.0) * d.oucf[i];
     } else {
       double yh = d.yhat[i];
@@ -162,24 +164,24 @@ struct EvalAEpi {
 };
 
 // KKT over A^T y_hat (utils.cu:503-531 variable half, plus objective dots)
-template <class T, bool LINF>
+template <class T, class M, bool LINF>
 struct EvalATEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 3;
   static constexpr unsigned MAXMASK = LINF ? 1u : 0u;
   Dev<T> d;
   PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return !d.ctl->done; }
-  __device__ T gather(int i) const { return d.yhat[i]; }
-  __device__ void row(int j, T s, double *acc) const {
+  __device__ M gather(int i) const { return (M)d.yhat[i]; }
+  __device__ void row(int j, M s, double *acc) const {
     double lam = d.lam[j], c = d.c[j];
     double dr = (c - (double)s - lam) * d.Dc[j];
     acc[0] = LINF ? fmax(acc[0], fabs(dr)) : acc[0] + dr * dr;
     if (d.shifted) {  // original objective at the centre plus the correction
-      double xo = d.sx[j] + (double)d.xhat[j] / (d.Dc[j] * d.cb);
+      double xo = d.sx[j] + (double)d.xhat[j] / (d.Dc[j] * d.cb) * d.sdp_inv;
       acc[1] += d.oc[j] * xo;
-      acc[2] += lam * d.Dc[j] / d.ob * xo;
+      acc[2] += lam * d.Dc[j] / d.ob * d.sdd_inv * xo;
     } else {
       double xh = d.xhat[j];
       acc[1] += c * xh;
@@ -194,10 +196,10 @@ __device__ __forceinline__ double ray_scale(const Ctl *c) {
 }
 
 // primal ray over A (utils.cu:561-572, :588-600)
-template <class T>
+template <class T, class M>
 struct InfAEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 2;
   static constexpr unsigned MAXMASK = 1u;
   Dev<T> d;
@@ -208,8 +210,8 @@ struct InfAEpi {
     sc = (T)ray_scale(d.ctl);
     return true;
   }
-  __device__ T gather(int j) const { return sc * d.dx[j]; }
-  __device__ void row(int i, T s, double *acc) const {
+  __device__ M gather(int j) const { return (M)(sc * d.dx[j]); }
+  __device__ void row(int i, M s, double *acc) const {
     double sd = s;
     double pi = (fmax(0.0, -sd) * (double)isfinite(d.lc[i]) +
                  fmax(0.0, sd) * (double)isfinite(d.uc[i])) * d.Dr[i];
@@ -221,10 +223,10 @@ struct InfAEpi {
 
 // dual ray over A^T (utils.cu:574-586, :602-614; the slack slot holds A^T dy
 // as in the reference call at utils.cu:772-776)
-template <class T>
+template <class T, class M>
 struct InfATEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 3;
   static constexpr unsigned MAXMASK = 2u;
   Dev<T> d;
@@ -235,8 +237,8 @@ struct InfATEpi {
     sc = (T)ray_scale(d.ctl);
     return true;
   }
-  __device__ T gather(int i) const { return d.dy[i]; }
-  __device__ void row(int j, T s, double *acc) const {
+  __device__ M gather(int i) const { return (M)d.dy[i]; }
+  __device__ void row(int j, M s, double *acc) const {
     double ns = -(double)s;
     acc[0] += fmax(ns, 0.0) * (double)d.lvf[j] + fmin(ns, 0.0) * (double)d.uvf[j];
     double di = (fmax(0.0, ns) * (double)!isfinite(d.lv[j]) -
@@ -247,18 +249,18 @@ struct InfATEpi {
 };
 
 // reduced cost (pdlp_core_op.cu:31-40), FP64 output in original units
-template <class T>
+template <class T, class M>
 struct ReducedCostEpi {
-  using val_t = T;
-  using acc_t = T;
+  using val_t = M;
+  using acc_t = M;
   static constexpr int NF = 0;
   static constexpr unsigned MAXMASK = 0;
   Dev<T> d;
   double *out;
   PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return true; }
-  __device__ T gather(int i) const { return d.yhat[i]; }
-  __device__ void row(int j, T s, double *) const {
+  __device__ M gather(int i) const { return (M)d.yhat[i]; }
+  __device__ void row(int j, M s, double *) const {
     out[j] = ((double)d.c[j] - (double)s) * d.Dc[j] / d.ob;
   }
 };

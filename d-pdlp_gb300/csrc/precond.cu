@@ -149,7 +149,8 @@ static int warp_grid(int rows) {
 
 void gpu_rescale(const pdhg_parameters_t &p, DevCsr &A, DevCsr &AT, double *c, double *lv,
                  double *uv, double *lc, double *uc, double *Dr, double *Dc, double *cb,
-                 double *ob, double *tmp_n, double *tmp_m, double *part, cudaStream_t st) {
+                 double *ob, double *tmp_n, double *tmp_m, double *part, cudaStream_t st,
+                 double fixed_cb, double fixed_ob) {
   const int n = A.cols, m = A.rows;
   const int gv = grid_for((long)n + m);
   k_fill<<<grid_for(m), kThreads, 0, st>>>(m, Dr, 1.0);
@@ -174,7 +175,17 @@ void gpu_rescale(const pdhg_parameters_t &p, DevCsr &A, DevCsr &AT, double *c, d
     PDLP_LAUNCH_CHECK();
     apply(tmp_m, tmp_n);
   }
-  if (p.bound_objective_rescaling) {
+  if (fixed_cb > 0.0 && fixed_ob > 0.0) {
+    // refinement rounds keep the first round's bound / objective scaling
+    double h[2] = {fixed_cb, fixed_ob};
+    double *out = part;
+    PDLP_CUDA(cudaMemcpyAsync(out, h, sizeof(h), cudaMemcpyHostToDevice, st));
+    k_scale_bounds_obj<<<gv, kThreads, 0, st>>>(n, m, c, lv, uv, lc, uc, out);
+    PDLP_LAUNCH_CHECK();
+    PDLP_CUDA(cudaStreamSynchronize(st));
+    *cb = fixed_cb;
+    *ob = fixed_ob;
+  } else if (p.bound_objective_rescaling) {
     int g = grid_for((long)n + m);
     if (g > kMiscPart / 2 - 2) g = kMiscPart / 2 - 2;
     double *out = part + 2 * g;

@@ -29,12 +29,13 @@ struct CorrAEpi {
   static constexpr unsigned MAXMASK = 0;
   const double *xbar, *lc, *uc;
   double *lc2, *uc2;
+  double dp;
   PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return true; }
   __device__ double gather(int j) const { return xbar[j]; }
   __device__ void row(int i, double s, double *) const {
-    lc2[i] = lc[i] - s;
-    uc2[i] = uc[i] - s;
+    lc2[i] = dp * (lc[i] - s);
+    uc2[i] = dp * (uc[i] - s);
   }
 };
 
@@ -46,14 +47,15 @@ struct CorrATEpi {
   static constexpr unsigned MAXMASK = 0;
   const double *ybar, *c, *lv, *uv, *xbar;
   double *c2, *lv2, *uv2;
+  double dp, dd;
   PDLP_NO_BLOCK_SCALARS
   __device__ bool init() { return true; }
   __device__ double gather(int i) const { return ybar[i]; }
   __device__ void row(int j, double s, double *) const {
-    c2[j] = c[j] - s;
+    c2[j] = dd * (c[j] - s);
     double xb = xbar[j];
-    lv2[j] = lv[j] - xb;
-    uv2[j] = uv[j] - xb;
+    lv2[j] = dp * (lv[j] - xb);
+    uv2[j] = dp * (uv[j] - xb);
   }
 };
 
@@ -91,15 +93,16 @@ __global__ void k_finite(int m, const double *lc, const double *uc, double *lcf,
 
 // xbar += z, ybar += w, keeping the previous point for a rollback
 __global__ void k_accumulate(int n, int m, double *xbar, double *ybar, double *xold,
-                             double *yold, const double *z, const double *w) {
+                             double *yold, const double *z, const double *w, double dpi,
+                             double ddi) {
   long stride = (long)gridDim.x * blockDim.x;
   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
     xold[j] = xbar[j];
-    xbar[j] += z[j];
+    xbar[j] += z[j] * dpi;
   }
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
     yold[i] = ybar[i];
-    ybar[i] += w[i];
+    ybar[i] += w[i] * ddi;
   }
 }
 
@@ -209,15 +212,29 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   int limit = params.termination_criteria.iteration_limit;
   Kkt kkt{};
   double best_err = INFINITY;
-  double omega0 = 1.0, cb0 = 1.0, ob0 = 1.0;
+  double omega0 = 1.0, cb0 = 1.0, ob0 = 1.0, dp = 1.0, dd = 1.0;
   reason = TERMINATION_REASON_ITERATION_LIMIT;  // unless a round meets the tolerances
   cupdlpx_result_t *ray_result = nullptr;
   double rescale_sec = 0.0;
   for (int round = 0; round < opt.max_rounds; ++round) {
     const DevProblem &R = round == 0 ? P : Q;
+    bool stop = false;
     if (round > 0) {
-      launch_spmv(A, CorrAEpi{xbar, P.lc, P.uc, lc2, uc2}, nullptr, nullptr, st);
-      launch_spmv(AT, CorrATEpi{ybar, P.c, P.lv, P.uv, xbar, c2, lv2, uv2}, nullptr, nullptr, st);
+      // unit-size correction: scale by the inverse of the current relative
+      // residuals (primal / dual+gap), never below 1
+      dp = 1.0 / fmax(fmax(kkt.rel_p, kkt.rel_gap), 0.1 * eps_feas);
+      dd = 1.0 / fmax(fmax(kkt.rel_d, kkt.rel_gap), 0.1 * eps_feas);
+      dp = fmax(dp, 1.0);
+      dd = fmax(dd, 1.0);
+      Q.delta_p = dp;
+      Q.delta_d = dd;
+      Q.cnorm_l2 = dd * (1.0 + P.cnorm_l2) - 1.0;
+      Q.cnorm_linf = dd * (1.0 + P.cnorm_linf) - 1.0;
+      Q.bnorm_l2 = dp * (1.0 + P.bnorm_l2) - 1.0;
+      Q.bnorm_linf = dp * (1.0 + P.bnorm_linf) - 1.0;
+      launch_spmv(A, CorrAEpi{xbar, P.lc, P.uc, lc2, uc2, dp}, nullptr, nullptr, st);
+      launch_spmv(AT, CorrATEpi{ybar, P.c, P.lv, P.uv, xbar, c2, lv2, uv2, dp, dd}, nullptr,
+                  nullptr, st);
       launches += 2;
     }
     pdhg_parameters_t pi = params;
@@ -231,67 +248,84 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
       pi.termination_criteria.eps_feasible_relative = opt.inner_eps > 0.0 ? e : e * eps_feas;
       pi.termination_criteria.eps_optimal_relative = opt.inner_eps > 0.0 ? e : e * eps_opt;
     }
-    Solve<float> s(pi, st, R, 0);
-    s.prepare();
-    if (round == 0) rescale_sec = s.rescale_seconds();
-    // the primal weight balances scaled primal and dual distances, so it
-    // carries over between rounds in proportion to ob / cb
-    double omega = round == 0 ? 0.0 : omega0 * (s.ob() / s.cb()) / (ob0 / cb0);
-    s.init_step(sigma, omega);
-    if (round == 0) {
-      sigma = s.sigma_max();
-      rep.power_iterations = s.power_iterations();
-      rep.sigma_max = sigma;
-    }
-    s.set_stall_rule(3000, 0.3);  // FP32 has a precision floor: every round must end
-    s.enable_snapshot();
-    s.run();
-    if (round == 0) {
-      omega0 = s.primal_weight();
-      cb0 = s.cb();
-      ob0 = s.ob();
-    }
-    int r = s.reason();
-    iters += s.total_count();
-    launches += s.kernel_launches();
-    rep.rounds = round + 1;
-    if (r == TERMINATION_REASON_PRIMAL_INFEASIBLE || r == TERMINATION_REASON_DUAL_INFEASIBLE) {
-      // infeasibility certificates come from the first round's FP32 rays
-      ray_result = s.result();
-      reason = r;
-      break;
-    }
-    s.result_device(z, w, lz);
-    k_accumulate<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold, z, w);
-    PDLP_LAUNCH_CHECK();
-    launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
-    launches += 2;
-    Kkt k = ev.evaluate(xbar, ybar, lam);
-    launches += 4;
-    double err = fmax(k.rel_p / eps_feas, fmax(k.rel_d / eps_feas, k.rel_gap / eps_opt));
-    if (params.verbose)
-      printf("refinement round %d: %d FP32 iterations (reason %d, primal weight %.3g) -> FP64 "
-             "rel primal %.3e rel dual %.3e rel gap %.3e\n",
-             round, s.total_count(), r, s.primal_weight(), k.rel_p, k.rel_d, k.rel_gap);
-    if (round > 0 && err >= best_err) {
-      // the round did not improve the FP64 point: keep the previous one
-      k_rollback<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold);
-      launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
+    // one round with either FP32 iterates or FP64 iterates over an FP32 matrix;
+    // returns true when the refinement should stop
+    auto round_body = [&](auto &s) -> bool {
+      // corrections keep the first round's bound / objective scaling, so the
+      // scaled correction looks like the scaled original near its optimum
+      if (round > 0) s.set_fixed_scaling(cb0, ob0);
+      s.prepare();
+      if (round == 0) rescale_sec = s.rescale_seconds();
+      // the primal weight balances the scaled dual and primal distances, which
+      // the correction multiplies by dd and dp
+      double omega = round == 0 ? 0.0 : omega0 * dd / dp;
+      s.init_step(sigma, omega);
+      if (round == 0) {
+        sigma = s.sigma_max();
+        rep.power_iterations = s.power_iterations();
+        rep.sigma_max = sigma;
+      }
+      s.set_stall_rule(10000, 0.5);  // a precision floor ends a round, never a hang
+      s.enable_snapshot();
+      s.run();
+      if (round == 0) {
+        omega0 = s.primal_weight();
+        cb0 = s.cb();
+        ob0 = s.ob();
+      }
+      int r = s.reason();
+      iters += s.total_count();
+      launches += s.kernel_launches();
+      rep.rounds = round + 1;
+      if (r == TERMINATION_REASON_PRIMAL_INFEASIBLE || r == TERMINATION_REASON_DUAL_INFEASIBLE) {
+        // infeasibility certificates come from the first round's rays
+        ray_result = s.result();
+        reason = r;
+        return true;
+      }
+      s.result_device(z, w, lz);
+      k_accumulate<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold, z,
+                                                               w, 1.0 / dp, 1.0 / dd);
       PDLP_LAUNCH_CHECK();
+      launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
       launches += 2;
-      break;
+      Kkt k = ev.evaluate(xbar, ybar, lam);
+      launches += 4;
+      double err = fmax(k.rel_p / eps_feas, fmax(k.rel_d / eps_feas, k.rel_gap / eps_opt));
+      if (params.verbose)
+        printf("refinement round %d: dp %.3g dd %.3g, %d iterations (reason %d, primal "
+               "weight %.3g) -> FP64 rel primal %.3e rel dual %.3e rel gap %.3e\n",
+               round, dp, dd, s.total_count(), r, s.primal_weight(), k.rel_p, k.rel_d,
+               k.rel_gap);
+      if (round > 0 && err >= best_err) {
+        // the round did not improve the FP64 point: keep the previous one
+        k_rollback<<<grid_for((long)n + m), kThreads, 0, st>>>(n, m, xbar, ybar, xold, yold);
+        launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
+        PDLP_LAUNCH_CHECK();
+        launches += 2;
+        return true;
+      }
+      best_err = err;
+      kkt = k;
+      if (err < 1.0) {
+        reason = TERMINATION_REASON_OPTIMAL;
+        return true;
+      }
+      if (r == TERMINATION_REASON_ITERATION_LIMIT || r == TERMINATION_REASON_TIME_LIMIT ||
+          iters >= limit) {
+        reason = r == TERMINATION_REASON_TIME_LIMIT ? r : TERMINATION_REASON_ITERATION_LIMIT;
+        return true;
+      }
+      return false;
+    };
+    if (opt.fp64_iterates) {
+      Solve<double, float> s(pi, st, R, 0);
+      stop = round_body(s);
+    } else {
+      Solve<float, float> s(pi, st, R, 0);
+      stop = round_body(s);
     }
-    best_err = err;
-    kkt = k;
-    if (err < 1.0) {
-      reason = TERMINATION_REASON_OPTIMAL;
-      break;
-    }
-    if (r == TERMINATION_REASON_ITERATION_LIMIT || r == TERMINATION_REASON_TIME_LIMIT ||
-        iters >= limit) {
-      reason = r == TERMINATION_REASON_TIME_LIMIT ? r : TERMINATION_REASON_ITERATION_LIMIT;
-      break;
-    }
+    if (stop) break;
   }
   (void)linf;
   double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -1,303 +1,16 @@
-// solver.cu -- restarted Halpern PDHG on one GPU (FP64 or FP32 iterates).
+// solver.cu -- problem upload and the FP64 instantiation of the PDHG solve.
 //
-// Per iteration two kernels run (reference src/solver.cu:85-102):
-//   primal : g = A^T y (fused SpMV) -> x_hat = proj(x - tau (c - g)),
-//            x_ref = 2 x_hat - x, Halpern x_next = w x_ref + (1-w) x0
-//            (reference pdlp_core_op.cu:393-418, :445-462, :495-526)
-//   dual   : h = A x_ref (fused SpMV) -> y_hat = sigma (t - proj(t)),
-//            t = y/sigma - h, y_ref = 2 y_hat - y, Halpern y_next
-//            (reference pdlp_core_op.cu:420-443, :528-557)
-// The Halpern update of the reference is a separate pass after both steps;
-// it only reads z_ref, z and z0 element-wise, so it is folded into the two
-// epilogues, with z ping-ponged between two buffers.
-//
-// Evaluations, restarts, the fixed-point error and the termination test run
-// on the device at the iterations the reference schedules them
-// (reference src/solver.cu:58-103), so no iteration waits on the host.
-// Chunks of iterations are captured once as CUDA graphs and replayed.
-#include <math.h>
-#include <stdlib.h>
-#include <string.h>
-
-#include <chrono>
-#include <random>
-
-#include "iter_kernels.cuh"
+// The iteration itself (kernels and the Solve driver) lives in
+// solver_impl.cuh; this file holds the pieces defined once: the non-template
+// kernels, the host transpose, the device-resident problem, and
+// Solve<double, double>.
+#include "solver_impl.cuh"
 
 namespace pdlp {
 
-// Evaluation modes of k_eval_fin.
-enum EvalMode { kEvalCheck = 0, kEvalIterLimit = 1, kEvalOnly = 2 };
-
-// ======================================================= element kernels
 __global__ void k_set_tbase(Ctl *ctl, int t) { ctl->t_base = t; }
 __global__ void k_loop_start(Ctl *ctl) { ctl->t_start_ns = global_ns(); }
 __global__ void k_set_steps(Ctl *c) { set_steps(c); }
-
-// Ray projection + infinity norms (utils.cu:533-559, :744-748)
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_ray_project(Dev<T> d) {
-  if (d.ctl->done) return;
-  __shared__ double red[24];
-  double a[2] = {0.0, 0.0};
-  long stride = (long)gridDim.x * kThreads;
-  for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
-    T v = d.dx[j];
-    if (isfinite(d.lv[j])) v = fmax(v, T(0));
-    if (isfinite(d.uv[j])) v = fmin(v, T(0));
-    d.dx[j] = v;
-    a[0] = fmax(a[0], fabs((double)v));
-  }
-  for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
-    T v = d.dy[i];
-    if (!isfinite(d.lc[i])) v = fmin(v, T(0));
-    if (!isfinite(d.uc[i])) v = fmax(v, T(0));
-    d.dy[i] = v;
-    a[1] = fmax(a[1], fabs((double)v));
-  }
-  block_reduce_fields<2, 3u>(a, red);
-  if (threadIdx.x == 0) {
-    d.p_i0[blockIdx.x] = a[0];
-    d.p_i0[gridDim.x + blockIdx.x] = a[1];
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_ray_project_fin(Dev<T> d) {
-  if (d.ctl->done) return;
-  __shared__ double sm[32];
-  double p = block_fold<true>(d.p_i0, d.ew_grid, sm);
-  double q = block_fold<true>(d.p_i0 + d.ew_grid, d.ew_grid, sm);
-  if (threadIdx.x == 0) {
-    d.ctl->ray_primal_inf_norm = p;
-    d.ctl->ray_dual_inf_norm = q;
-  }
-}
-
-// Restart copy + distances (pdlp_core_op.cu:577-591, :621-632)
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_restart(Dev<T> d, T *xcur, T *ycur) {
-  if (d.ctl->done || !d.ctl->do_restart) return;
-  __shared__ double red[24];
-  double a[2] = {0.0, 0.0};
-  long stride = (long)gridDim.x * kThreads;
-  for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
-    T xh = d.xhat[j];
-    double dd = (double)xh - (double)d.x0[j];
-    a[0] += dd * dd;
-    d.x0[j] = xh;
-    xcur[j] = xh;
-  }
-  for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
-    T yh = d.yhat[i];
-    double dd = (double)yh - (double)d.y0[i];
-    a[1] += dd * dd;
-    d.y0[i] = yh;
-    ycur[i] = yh;
-  }
-  block_reduce_fields<2, 0u>(a, red);
-  if (threadIdx.x == 0) {
-    d.p_rs[blockIdx.x] = a[0];
-    d.p_rs[gridDim.x + blockIdx.x] = a[1];
-  }
-}
-
-// PID primal-weight update (pdlp_core_op.cu:593-619)
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_restart_fin(Dev<T> d, int off) {
-  Ctl *c = d.ctl;
-  if (c->done || !c->do_restart) return;
-  __shared__ double sm[32];
-  double ps = block_fold<false>(d.p_rs, d.ew_grid, sm);
-  double ds = block_fold<false>(d.p_rs + d.ew_grid, d.ew_grid, sm);
-  if (threadIdx.x != 0) return;
-  double pd = sqrt(ps), dd = sqrt(ds);
-  double ratio = c->rel_dual_res / c->rel_primal_res;
-  if (pd > 1e-16 && dd > 1e-16 && pd < 1e12 && dd < 1e12 && ratio > 1e-8 && ratio < 1e8) {
-    double err = log(dd) - log(pd) - log(c->primal_weight);
-    c->pw_error_sum *= d.ismooth;
-    c->pw_error_sum += err;
-    double derr = err - c->pw_last_error;
-    c->primal_weight *= exp(d.kp * err + d.ki * c->pw_error_sum + d.kd * derr);
-    c->pw_last_error = err;
-  } else {
-    c->primal_weight = c->best_primal_weight;
-    c->pw_error_sum = 0.0;
-    c->pw_last_error = 0.0;
-  }
-  double g = fabs(log10(c->rel_dual_res / c->rel_primal_res));
-  if (g < c->best_gap) {
-    c->best_gap = g;
-    c->best_primal_weight = c->primal_weight;
-  }
-  set_steps(c);
-  c->restart_t = c->t_base + off;
-  c->last_trial_fixed_point_error = INFINITY;
-}
-
-// Fixed-point error (pdlp_core_op.cu:677-695) + restart bookkeeping
-// (solver.cu:89-95)
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_fpe_fin(Dev<T> d, int restart_only) {
-  Ctl *c = d.ctl;
-  if (c->done) return;
-  if (restart_only && !c->do_restart) return;
-  __shared__ double sm[32];
-  double pn2 = fold_site<false>(d.p_pstep, d.nblkT, d.lp_pstep, d.nlongT, 0, sm);
-  double dn2 = fold_site<false>(d.p_dstep, d.nblkA, d.lp_dstep, d.nlongA, 0, sm);
-  double cross = fold_site<false>(d.p_fpe, d.nblkT, d.lp_fpe, d.nlongT, 0, sm);
-  if (threadIdx.x != 0) return;
-  double pn = sqrt(pn2), dn = sqrt(dn2);
-  double w = c->primal_weight;
-  double movement = pn * pn * w + dn * dn / w;
-  double interaction = 2 * c->step_size * cross;
-  c->fixed_point_error = sqrt(movement + interaction);
-  if (c->do_restart) {
-    c->initial_fixed_point_error = c->fixed_point_error;
-    c->do_restart = 0;
-  }
-}
-
-// Evaluation: KKT scalars, optional ray statistics, termination test,
-// restart decision, trace record (utils.cu:639-813, :239-293; solver.cu:59-83)
-template <class T>
-__global__ void __launch_bounds__(kThreads)
-    k_eval_fin(Dev<T> d, int off, int infeas, int restart_check, int mode) {
-  Ctl *c = d.ctl;
-  if (c->done) return;
-  __shared__ double sm[32];
-  const bool L = d.linf != 0;
-  double pr = L ? fold_site<true>(d.p_e1, d.nblkA, d.lp_e1, d.nlongA, 0, sm)
-                : fold_site<false>(d.p_e1, d.nblkA, d.lp_e1, d.nlongA, 0, sm);
-  double qsum = fold_site<false>(d.p_e1, d.nblkA, d.lp_e1, d.nlongA, 1, sm);
-  double dr = L ? fold_site<true>(d.p_e2, d.nblkT, d.lp_e2, d.nlongT, 0, sm)
-                : fold_site<false>(d.p_e2, d.nblkT, d.lp_e2, d.nlongT, 0, sm);
-  double cx = fold_site<false>(d.p_e2, d.nblkT, d.lp_e2, d.nlongT, 1, sm);
-  double lx = fold_site<false>(d.p_e2, d.nblkT, d.lp_e2, d.nlongT, 2, sm);
-  double i1max = 0, i1sum = 0, i2sum = 0, i2max = 0, i2c = 0;
-  if (infeas) {
-    i1max = fold_site<true>(d.p_i1, d.nblkA, d.lp_i1, d.nlongA, 0, sm);
-    i1sum = fold_site<false>(d.p_i1, d.nblkA, d.lp_i1, d.nlongA, 1, sm);
-    i2sum = fold_site<false>(d.p_i2, d.nblkT, d.lp_i2, d.nlongT, 0, sm);
-    i2max = fold_site<true>(d.p_i2, d.nblkT, d.lp_i2, d.nlongT, 1, sm);
-    i2c = fold_site<false>(d.p_i2, d.nblkT, d.lp_i2, d.nlongT, 2, sm);
-  }
-  if (threadIdx.x != 0) return;
-  const int t = c->t_base + off;
-  const double cbo = d.cb * d.ob;
-  c->abs_primal_res = (L ? pr : sqrt(pr)) / d.cb;
-  c->abs_dual_res = (L ? dr : sqrt(dr)) / d.ob;
-  if (d.shifted) {  // terms already in original units
-    c->primal_obj = cx + d.oc0;
-    c->dual_obj = lx + qsum + d.oc0;
-  } else {
-    c->primal_obj = cx / cbo + d.c0;
-    c->dual_obj = (lx + qsum) / cbo + d.c0;
-  }
-  c->rel_primal_res = c->abs_primal_res / (1.0 + d.bnorm);
-  c->rel_dual_res = c->abs_dual_res / (1.0 + d.cnorm);
-  c->gap = fabs(c->primal_obj - c->dual_obj);
-  c->rel_gap = c->gap / (1.0 + fabs(c->primal_obj) + fabs(c->dual_obj));
-  if (mode == kEvalOnly) return;
-  if (infeas) {
-    c->primal_ray_obj = i2c / cbo;
-    c->dual_ray_obj = (i1sum + i2sum) / cbo;
-    c->max_primal_ray_inf = i1max;
-    c->max_dual_ray_inf = i2max;
-    double scale = fmax(c->ray_dual_inf_norm, i2max);
-    if (scale > 0.0) {
-      c->max_dual_ray_inf /= scale;
-      c->dual_ray_obj /= scale;
-    } else {
-      c->max_dual_ray_inf = 0.0;
-      c->dual_ray_obj = 0.0;
-    }
-  }
-  c->cum_time = (double)(global_ns() - c->t_start_ns) * 1e-9;
-  int reason = TERMINATION_REASON_UNSPECIFIED;
-  bool stalled = false;
-  if (d.stall_min > 0 && mode == kEvalCheck) {
-    // best-iterate snapshot and stall rule of the refinement rounds
-    double err = fmax(c->rel_primal_res, fmax(c->rel_dual_res, c->rel_gap));
-    c->snap_now = err < c->snap_err ? 1 : 0;
-    if (c->snap_now) c->snap_err = err;
-    if (err < 0.9 * c->best_err) {
-      c->best_err = err;
-      c->best_err_t = t;
-    } else if (t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
-      stalled = true;
-    }
-  }
-  if (mode == kEvalIterLimit) {
-    reason = TERMINATION_REASON_ITERATION_LIMIT;
-  } else if (c->rel_dual_res < d.eps_feas && c->rel_primal_res < d.eps_feas &&
-             c->rel_gap < d.eps_opt) {
-    reason = TERMINATION_REASON_OPTIMAL;
-  } else if (c->dual_ray_obj > 0.0 && c->max_dual_ray_inf / c->dual_ray_obj <= d.eps_inf) {
-    reason = TERMINATION_REASON_PRIMAL_INFEASIBLE;
-  } else if (c->primal_ray_obj < 0.0 &&
-             c->max_primal_ray_inf / (-c->primal_ray_obj) <= d.eps_inf) {
-    reason = TERMINATION_REASON_DUAL_INFEASIBLE;
-  } else if (c->cum_time >= d.time_limit) {
-    reason = TERMINATION_REASON_TIME_LIMIT;
-  } else if (stalled) {
-    reason = kReasonStalled;
-  }
-  if (d.trace && c->trace_len < d.trace_cap) {
-    double *r = d.trace + (long)c->trace_len * 10;
-    r[0] = t;
-    r[1] = c->rel_primal_res;
-    r[2] = c->rel_dual_res;
-    r[3] = c->rel_gap;
-    r[4] = c->primal_obj;
-    r[5] = c->dual_obj;
-    r[6] = c->primal_weight;
-    r[7] = c->fixed_point_error;
-    r[8] = c->step_size;
-    r[9] = t - c->restart_t;
-    c->trace_len++;
-  }
-  if (d.verbose && t % print_frequency(t) == 0)
-    printf("%6d %.1e | %8.1e  %8.1e | %.1e %.1e %.1e | %.1e %.1e %.1e \n", t, c->cum_time,
-           c->primal_obj, c->dual_obj, c->abs_primal_res, c->abs_dual_res, c->gap,
-           c->rel_primal_res, c->rel_dual_res, c->rel_gap);
-  if (reason != TERMINATION_REASON_UNSPECIFIED) {
-    c->reason = reason;
-    c->final_t = t;
-    c->done = 1;
-    __threadfence_system();
-    d.hflag->done = 1;
-    return;
-  }
-  if (restart_check) {
-    // should_do_adaptive_restart (utils.cu:265-293)
-    bool r = false;
-    int inner = t - c->restart_t;
-    if (t == d.F) {
-      r = true;
-    } else if (t > d.F) {
-      double f = c->fixed_point_error, f0 = c->initial_fixed_point_error;
-      if (f <= d.suff * f0) r = true;
-      if (f <= d.nec * f0 && f > c->last_trial_fixed_point_error) r = true;
-      if (inner >= d.art * t) r = true;
-    }
-    c->last_trial_fixed_point_error = c->fixed_point_error;
-    c->do_restart = r ? 1 : 0;
-  }
-}
-
-// Copy the evaluated iterate into the snapshot when it is the best so far.
-template <class T>
-__global__ void k_snapshot(Dev<T> d) {
-  if (!d.ctl->snap_now) return;
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
-    d.bx[j] = d.xhat[j];
-    d.bl[j] = d.lam[j];
-  }
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
-    d.by[i] = d.yhat[i];
-}
 
 // ---- power method element kernels (utils.cu:107-153), FP64
 __global__ void __launch_bounds__(kThreads) k_pm_norm(PowDev d, const double *v) {
@@ -363,100 +76,6 @@ __global__ void __launch_bounds__(kThreads) k_pm_resid_fin(PowDev d) {
     }
   }
 }
-
-// Unscale (pdlp_core_op.cu:464-480) into FP64 outputs; the dual slack maps
-// back like the reduced cost (times Dc / ob).
-template <class T>
-__global__ void k_unscale(Dev<T> d, double *x, double *y, double *lam) {
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
-    x[j] = (double)d.xhat[j] / d.Dc[j] / d.cb;
-    if (lam) lam[j] = (double)d.lam[j] * d.Dc[j] / d.ob;
-  }
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
-    y[i] = (double)d.yhat[i] / d.Dr[i] / d.ob;
-}
-
-// Scale an original-units point into this solve's scaled space.
-template <class T>
-__global__ void k_scale_point(Dev<T> d, const double *x, const double *y, const double *lam) {
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < d.n; j += stride) {
-    d.xhat[j] = (T)(x[j] * d.Dc[j] * d.cb);
-    d.lam[j] = (T)(lam[j] * d.ob / d.Dc[j]);
-  }
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < d.m; i += stride)
-    d.yhat[i] = (T)(y[i] * d.Dr[i] * d.ob);
-}
-
-// Finite copies of the scaled bounds (pdlp_core_op.cu:203-230)
-template <class T>
-__global__ void k_finite_copies(int n, int m, const T *lv, const T *uv, const T *lc,
-                                const T *uc, T *lvf, T *uvf, T *lcf, T *ucf) {
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
-    lvf[j] = isfinite(lv[j]) ? lv[j] : T(0);
-    uvf[j] = isfinite(uv[j]) ? uv[j] : T(0);
-  }
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
-    lcf[i] = isfinite(lc[i]) ? lc[i] : T(0);
-    ucf[i] = isfinite(uc[i]) ? uc[i] : T(0);
-  }
-}
-
-// Warm start scaling (pdlp_core_op.cu:174-201)
-template <class T>
-__global__ void k_warm_start(int n, int m, const double *xs, const double *ys,
-                             const double *Dc, const double *Dr, double cb, double ob, T *x0,
-                             T *x, T *xhat, T *y0, T *y, T *yhat) {
-  long stride = (long)gridDim.x * blockDim.x;
-  if (xs)
-    for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += stride) {
-      T v = (T)(xs[j] * Dc[j] * cb);
-      x0[j] = v;
-      x[j] = v;
-      xhat[j] = v;
-    }
-  if (ys)
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += stride) {
-      T v = (T)(ys[i] * Dr[i] * ob);
-      y0[i] = v;
-      y[i] = v;
-      yhat[i] = v;
-    }
-}
-
-// FP64 -> T copy (rounding to nearest)
-template <class T>
-__global__ void k_convert(long n, const double *__restrict__ src, T *__restrict__ dst) {
-  long stride = (long)gridDim.x * blockDim.x;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride)
-    dst[i] = (T)src[i];
-}
-
-// ============================================================ host side
-namespace {
-size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
-
-struct Arena {
-  char *base = nullptr;
-  size_t off = 0;
-  template <class T>
-  T *take(size_t count) {
-    T *p = reinterpret_cast<T *>(base + off);
-    off += align256(count * sizeof(T) + 1);
-    return p;
-  }
-};
-
-struct Sizer {
-  size_t bytes = 0;
-  template <class T>
-  void add(size_t count) {
-    bytes += align256(count * sizeof(T) + 1);
-  }
-};
-}  // namespace
 
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
                     std::vector<int> &tp, std::vector<int> &tj,
@@ -611,595 +230,7 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   return P.release();
 }
 
-template <class T>
-Solve<T>::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
-                int trace_cap)
-    : p_(params), st_(stream), P_(prob), trace_cap_(trace_cap) {
-  alloc();
-}
 
-template <class T>
-Solve<T>::~Solve() {
-  if (snap_mem_) cudaFree(snap_mem_);
-  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
-  for (auto g : raw_graphs_) cudaGraphDestroy(g);
-  if (arena_) cudaFree(arena_);
-  if (hflag_) cudaFreeHost(hflag_);
-}
-
-template <class T>
-void Solve<T>::alloc() {
-  constexpr bool F64 = sizeof(T) == 8;
-  const int n = P_.n, m = P_.m, nnz = P_.nnz;
-  const int ew = grid_for((long)n + m, 4);
-  const size_t vn = n, vm = m;
-  const size_t nbA = P_.A.plan.nblk, nbT = P_.AT.plan.nblk;
-  const size_t nlA = P_.A.plan.nlong, nlT = P_.AT.plan.nlong;
-  Sizer z;
-  z.add<double>(nnz); z.add<double>(nnz);                      // FP64 scaled values
-  if (!F64) { z.add<T>(nnz); z.add<T>(nnz); }                  // iteration values
-  z.add<unsigned>(nlA); z.add<double>(nbA); z.add<unsigned>(nlT); z.add<double>(nbT);
-  for (int i = 0; i < 3; ++i) z.add<double>(vn);               // c lv uv (FP64 scaled)
-  for (int i = 0; i < 2; ++i) z.add<double>(vm);               // lc uc
-  z.add<double>(vn); z.add<double>(vm);                        // Dc Dr
-  if (!F64) {
-    for (int i = 0; i < 3; ++i) z.add<T>(vn);
-    for (int i = 0; i < 2; ++i) z.add<T>(vm);
-  }
-  for (int i = 0; i < 2; ++i) z.add<T>(vn);                    // lvf uvf
-  for (int i = 0; i < 2; ++i) z.add<T>(vm);                    // lcf ucf
-  for (int i = 0; i < 8; ++i) z.add<T>(vn);                    // x[2] x0 xref xhat lam dx auxn
-  for (int i = 0; i < 6; ++i) z.add<T>(vm);                    // y[2] y0 yhat dy auxm
-  z.add<double>(vm); z.add<double>(vm); z.add<double>(vn);     // power v[2], g
-  z.add<double>(vn); z.add<double>(vm); z.add<double>(vn);     // FP64 outputs x, y, rc/lam
-  size_t pa = nbA + nlA + 2, pt = nbT + nlT + 2;
-  z.add<double>(pt); z.add<double>(pa); z.add<double>(pt);    // pstep dstep fpe
-  z.add<double>(pa * 2); z.add<double>(pt * 3);               // e1 e2
-  z.add<double>((size_t)ew * 2);                               // i0
-  z.add<double>(pa * 2); z.add<double>(pt * 3);               // i1 i2
-  z.add<double>((size_t)ew * 2);                               // rs
-  z.add<double>(pa * 2); z.add<double>((size_t)ew);           // power partials
-  z.add<double>((size_t)kMiscPart);
-  z.add<Ctl>(1); z.add<double>((size_t)trace_cap_ * 10 + 1);
-  PDLP_CUDA(cudaMalloc(&arena_, z.bytes));
-  Arena ar{(char *)arena_, 0};
-
-  auto mat64 = [&](DevCsr &W, const DevCsr &S) {
-    W = S;
-    W.val = ar.take<double>(nnz);
-    W.plan.lcnt = ar.take<unsigned>(S.plan.nlong);
-    W.plan.lsum = ar.take<double>(S.plan.nblk);
-    if (S.plan.nlong) PDLP_CUDA(cudaMemsetAsync(W.plan.lcnt, 0, (size_t)S.plan.nlong * 4, st_));
-  };
-  mat64(A64_, P_.A);
-  mat64(AT64_, P_.AT);
-  auto matT = [&](DevCsrT<T> &W, const DevCsr &S64) {
-    W.rows = S64.rows;
-    W.cols = S64.cols;
-    W.nnz = S64.nnz;
-    W.ptr = S64.ptr;
-    W.col = S64.col;
-    W.plan = S64.plan;  // shares the per-solve scratch of the FP64 copy
-    if constexpr (F64) W.val = (T *)S64.val;
-    else W.val = ar.take<T>(nnz);
-  };
-  matT(A_, A64_);
-  matT(AT_, AT64_);
-
-  Dev<T> &d = d_;
-  d.n = n;
-  d.m = m;
-  c64_ = ar.take<double>(vn); lv64_ = ar.take<double>(vn); uv64_ = ar.take<double>(vn);
-  lc64_ = ar.take<double>(vm); uc64_ = ar.take<double>(vm);
-  d.Dc = ar.take<double>(vn);
-  d.Dr = ar.take<double>(vm);
-  if constexpr (F64) {
-    d.c = (const T *)c64_; d.lv = (const T *)lv64_; d.uv = (const T *)uv64_;
-    d.lc = (const T *)lc64_; d.uc = (const T *)uc64_;
-  } else {
-    d.c = ar.take<T>(vn); d.lv = ar.take<T>(vn); d.uv = ar.take<T>(vn);
-    d.lc = ar.take<T>(vm); d.uc = ar.take<T>(vm);
-  }
-  d.lvf = ar.take<T>(vn); d.uvf = ar.take<T>(vn);
-  d.lcf = ar.take<T>(vm); d.ucf = ar.take<T>(vm);
-  d.x[0] = ar.take<T>(vn); d.x[1] = ar.take<T>(vn); d.x0 = ar.take<T>(vn);
-  d.xref = ar.take<T>(vn); d.xhat = ar.take<T>(vn); d.lam = ar.take<T>(vn);
-  d.dx = ar.take<T>(vn); d.auxn = ar.take<T>(vn);
-  d.y[0] = ar.take<T>(vm); d.y[1] = ar.take<T>(vm); d.y0 = ar.take<T>(vm);
-  d.yhat = ar.take<T>(vm); d.dy = ar.take<T>(vm); d.auxm = ar.take<T>(vm);
-  pw_.v[0] = ar.take<double>(vm); pw_.v[1] = ar.take<double>(vm); pw_.g = ar.take<double>(vn);
-  outx_ = ar.take<double>(vn); outy_ = ar.take<double>(vm); outl_ = ar.take<double>(vn);
-  d.nblkA = (int)nbA; d.nlongA = (int)nlA; d.nblkT = (int)nbT; d.nlongT = (int)nlT;
-  d.ew_grid = ew;
-  auto split = [&](double *&p, double *&lp, size_t nb, size_t nl, int nf) {
-    double *base = ar.take<double>((nb + nl + 2) * nf);
-    p = base;
-    lp = base + nb * nf;
-  };
-  split(d.p_pstep, d.lp_pstep, nbT, nlT, 1);
-  split(d.p_dstep, d.lp_dstep, nbA, nlA, 1);
-  split(d.p_fpe, d.lp_fpe, nbT, nlT, 1);
-  split(d.p_e1, d.lp_e1, nbA, nlA, 2);
-  split(d.p_e2, d.lp_e2, nbT, nlT, 3);
-  d.p_i0 = ar.take<double>((size_t)ew * 2);
-  split(d.p_i1, d.lp_i1, nbA, nlA, 2);
-  split(d.p_i2, d.lp_i2, nbT, nlT, 3);
-  d.p_rs = ar.take<double>((size_t)ew * 2);
-  split(pw_.p_pa, pw_.lp_pa, nbA, nlA, 2);
-  pw_.p_pr = ar.take<double>((size_t)ew);
-  d.p_misc = ar.take<double>((size_t)kMiscPart);
-  d.ctl = ar.take<Ctl>(1);
-  d.trace = trace_cap_ > 0 ? ar.take<double>((size_t)trace_cap_ * 10) : nullptr;
-  d.trace_cap = trace_cap_;
-
-  PDLP_CUDA(cudaHostAlloc((void **)&hflag_, sizeof(HostFlag), cudaHostAllocMapped));
-  hflag_->done = 0;
-  hflag_->pm_done = 0;
-  HostFlag *dflag = nullptr;
-  PDLP_CUDA(cudaHostGetDevicePointer((void **)&dflag, hflag_, 0));
-  d.hflag = dflag;
-
-  pw_.n = n;
-  pw_.m = m;
-  pw_.ctl = d.ctl;
-  pw_.hflag = dflag;
-  pw_.nblkA = (int)nbA;
-  pw_.nlongA = (int)nlA;
-  pw_.ew_grid = ew;
-}
-
-template <class T>
-void Solve<T>::prepare() {
-  Dev<T> &d = d_;
-  const int n = d.n, m = d.m, nnz = P_.nnz;
-  auto t0 = std::chrono::steady_clock::now();
-  d.c0 = P_.c0;
-  d.shifted = P_.shift_x != nullptr;
-  d.sx = P_.shift_x;
-  d.sy = P_.shift_y;
-  d.oc = P_.orig_c;
-  d.olcf = P_.orig_lcf;
-  d.oucf = P_.orig_ucf;
-  d.oc0 = P_.orig_c0;
-  d.rho = p_.reflection_coefficient;
-  d.one_minus_rho = 1.0 - d.rho;
-  d.rho_is_one = d.rho == 1.0;
-  d.F = p_.termination_evaluation_frequency > 0 ? p_.termination_evaluation_frequency : 1;
-  d.linf = p_.optimality_norm == NORM_TYPE_L_INF;
-  d.cnorm = d.linf ? P_.cnorm_linf : P_.cnorm_l2;
-  d.bnorm = d.linf ? P_.bnorm_linf : P_.bnorm_l2;
-  d.verbose = p_.verbose;
-  d.eps_opt = p_.termination_criteria.eps_optimal_relative;
-  d.eps_feas = p_.termination_criteria.eps_feasible_relative;
-  d.eps_inf = p_.termination_criteria.eps_infeasible;
-  d.time_limit = p_.termination_criteria.time_sec_limit;
-  d.art = p_.restart_params.artificial_restart_threshold;
-  d.suff = p_.restart_params.sufficient_reduction_for_restart;
-  d.nec = p_.restart_params.necessary_reduction_for_restart;
-  d.kp = p_.restart_params.k_p;
-  d.ki = p_.restart_params.k_i;
-  d.kd = p_.restart_params.k_d;
-  d.ismooth = p_.restart_params.i_smooth;
-  pw_.sv_tol = p_.sv_tol;
-  auto d2d = [&](const void *dst, const void *src, size_t b) {
-    if (b) PDLP_CUDA(cudaMemcpyAsync((void *)dst, src, b, cudaMemcpyDeviceToDevice, st_));
-  };
-  d2d(A64_.val, P_.A.val, (size_t)nnz * 8);
-  d2d(AT64_.val, P_.AT.val, (size_t)nnz * 8);
-  d2d(c64_, P_.c, (size_t)n * 8);
-  d2d(lv64_, P_.lv, (size_t)n * 8);
-  d2d(uv64_, P_.uv, (size_t)n * 8);
-  d2d(lc64_, P_.lc, (size_t)m * 8);
-  d2d(uc64_, P_.uc, (size_t)m * 8);
-  gpu_rescale(p_, A64_, AT64_, c64_, lv64_, uv64_, lc64_, uc64_, (double *)d.Dr,
-              (double *)d.Dc, &d.cb, &d.ob, outx_, outy_, d.p_misc, st_);
-  int g = grid_for((long)n + m);
-  if constexpr (sizeof(T) != 8) {
-    int gz = grid_for(nnz);
-    k_convert<T><<<gz, kThreads, 0, st_>>>(nnz, A64_.val, A_.val);
-    k_convert<T><<<gz, kThreads, 0, st_>>>(nnz, AT64_.val, AT_.val);
-    int gn = grid_for(n), gm = grid_for(m);
-    k_convert<T><<<gn, kThreads, 0, st_>>>(n, c64_, (T *)d.c);
-    k_convert<T><<<gn, kThreads, 0, st_>>>(n, lv64_, (T *)d.lv);
-    k_convert<T><<<gn, kThreads, 0, st_>>>(n, uv64_, (T *)d.uv);
-    k_convert<T><<<gm, kThreads, 0, st_>>>(m, lc64_, (T *)d.lc);
-    k_convert<T><<<gm, kThreads, 0, st_>>>(m, uc64_, (T *)d.uc);
-    PDLP_LAUNCH_CHECK();
-  }
-  k_finite_copies<T><<<g, kThreads, 0, st_>>>(n, m, d.lv, d.uv, d.lc, d.uc, (T *)d.lvf,
-                                              (T *)d.uvf, (T *)d.lcf, (T *)d.ucf);
-  PDLP_LAUNCH_CHECK();
-  for (T *p : {d.x[0], d.x[1], d.x0, d.xref, d.xhat, d.lam, d.dx})
-    if (n) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)n * sizeof(T), st_));
-  for (T *p : {d.y[0], d.y[1], d.y0, d.yhat, d.dy})
-    if (m) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)m * sizeof(T), st_));
-  if (P_.xs || P_.ys) {
-    k_warm_start<T><<<g, kThreads, 0, st_>>>(n, m, P_.xs, P_.ys, d.Dc, d.Dr, d.cb, d.ob, d.x0,
-                                             d.x[0], d.xhat, d.y0, d.y[0], d.yhat);
-    PDLP_LAUNCH_CHECK();
-  }
-  Ctl c0;
-  memset(&c0, 0, sizeof(c0));
-  c0.best_gap = INFINITY;
-  c0.last_trial_fixed_point_error = INFINITY;
-  c0.reason = TERMINATION_REASON_UNSPECIFIED;
-  c0.step_size = 1.0;
-  c0.primal_weight = 1.0;
-  c0.best_primal_weight = 1.0;
-  c0.tau = c0.sigma = c0.inv_sigma = 1.0;
-  c0.best_err = INFINITY;
-  c0.snap_err = INFINITY;
-  PDLP_CUDA(cudaMemcpyAsync(d.ctl, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-  hflag_->done = 0;
-  hflag_->pm_done = 0;
-  rescale_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-}
-
-template <class T>
-void Solve<T>::power_method() {
-  PowDev &w = pw_;
-  const int m = w.m;
-  // start vector: m draws of N(0,1) from a fresh mt19937(1), like the
-  // reference's first solve in a process (utils.cu:29-30, :79-82)
-  std::vector<double> v0(m);
-  {
-    std::mt19937 gen(1);
-    std::normal_distribution<double> dist(0.0, 1.0);
-    for (int i = 0; i < m; ++i) v0[i] = dist(gen);
-  }
-  PDLP_CUDA(cudaMemcpyAsync(w.v[0], v0.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st_));
-  k_pm_norm<<<w.ew_grid, kThreads, 0, st_>>>(w, w.v[0]);
-  k_pm_norm_fin<<<1, kThreads, 0, st_>>>(w);
-  PDLP_LAUNCH_CHECK();
-  launches_ += 2;
-  // chunks of power iterations, captured once and replayed until converged
-  const int CH = 16;
-  auto enqueue = [&](int it) {
-    const double *v = w.v[it & 1];
-    double *vn = w.v[(it + 1) & 1];
-    launch_spmv(AT64_, PowAtEpi{w, v, 0.0}, nullptr, nullptr, st_);
-    launch_spmv(A64_, PowAEpi{w, v, vn, 0.0}, w.p_pa, w.lp_pa, st_);
-    k_pm_dot_fin<<<1, kThreads, 0, st_>>>(w);
-    k_pm_resid<<<w.ew_grid, kThreads, 0, st_>>>(w, v, vn);
-    k_pm_resid_fin<<<1, kThreads, 0, st_>>>(w);
-    PDLP_LAUNCH_CHECK();
-  };
-  cudaGraph_t graph;
-  cudaGraphExec_t exec;
-  PDLP_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < CH; ++i) enqueue(i);
-  PDLP_CUDA(cudaStreamEndCapture(st_, &graph));
-  PDLP_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  int launched = 0;
-  const int maxit = p_.sv_max_iter;
-  while (launched + CH <= maxit) {
-    PDLP_CUDA(cudaGraphLaunch(exec, st_));
-    launched += CH;
-    launches_ += CH * 5;
-    PDLP_CUDA(cudaStreamSynchronize(st_));
-    if (hflag_->pm_done) break;
-  }
-  if (!hflag_->pm_done)
-    for (int i = launched; i < maxit; ++i) {  // even CH: parity restarts at 0
-      enqueue(i - launched);
-      launches_ += 5;
-    }
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
-  Ctl c;
-  PDLP_CUDA(cudaMemcpyAsync(&c, w.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-  pm_iters_ = c.pm_iters;
-  sigma_max_ = sqrt(c.pm_sigma_sq);
-}
-
-template <class T>
-void Solve<T>::init_step(double known_sigma, double known_omega) {
-  Dev<T> &d = d_;
-  double eta = 1.0;
-  if (A64_.nnz > 0 && d.m > 0) {
-    if (known_sigma > 0.0) sigma_max_ = known_sigma;
-    else power_method();
-    eta = 0.998 / sigma_max_;
-  }
-  double omega = p_.bound_objective_rescaling ? 1.0 : (d.cnorm + 1.0) / (d.bnorm + 1.0);
-  if (known_omega > 0.0) omega = known_omega;
-  // ctl offsets of step_size/primal_weight/best_primal_weight are the first 3 doubles
-  double s[3] = {eta, omega, omega};
-  PDLP_CUDA(cudaMemcpyAsync(d.ctl, s, sizeof(s), cudaMemcpyHostToDevice, st_));
-  k_set_steps<<<1, 1, 0, st_>>>(d.ctl);
-  PDLP_LAUNCH_CHECK();
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-}
-
-template <class T>
-void Solve<T>::enqueue_eval(int off, bool infeas, bool restart_check, int mode) {
-  Dev<T> &d = d_;
-  if (d.linf) {
-    launch_spmv(A_, EvalAEpi<T, true>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<T, true>{d}, d.p_e2, d.lp_e2, st_);
-  } else {
-    launch_spmv(A_, EvalAEpi<T, false>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<T, false>{d}, d.p_e2, d.lp_e2, st_);
-  }
-  if (infeas) {
-    k_ray_project<T><<<d.ew_grid, kThreads, 0, st_>>>(d);
-    k_ray_project_fin<T><<<1, kThreads, 0, st_>>>(d);
-    launch_spmv(A_, InfAEpi<T>{d, T(0)}, d.p_i1, d.lp_i1, st_);
-    launch_spmv(AT_, InfATEpi<T>{d, T(0)}, d.p_i2, d.lp_i2, st_);
-  }
-  k_eval_fin<T><<<1, kThreads, 0, st_>>>(d, off, infeas, restart_check, mode);
-  PDLP_LAUNCH_CHECK();
-  if (snapshot_ && mode == kEvalCheck) {
-    k_snapshot<T><<<d.ew_grid, kThreads, 0, st_>>>(d);
-    PDLP_LAUNCH_CHECK();
-  }
-}
-
-template <class T>
-void Solve<T>::enable_snapshot() {
-  if (snapshot_) return;
-  Dev<T> &d = d_;
-  size_t bytes = ((size_t)d.n * 2 + d.m) * sizeof(T) + 1024;
-  void *mem = nullptr;
-  PDLP_CUDA(cudaMalloc(&mem, bytes));
-  snap_mem_ = mem;
-  d.bx = (T *)mem;
-  d.bl = d.bx + d.n;
-  d.by = d.bl + d.n;
-  snapshot_ = true;
-}
-
-template <class T>
-double Solve<T>::primal_weight() const {
-  Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  return c.primal_weight;
-}
-
-template <class T>
-void Solve<T>::enqueue_iteration(int t, int off) {
-  Dev<T> &d = d_;
-  IterFlags f = iteration_flags(t, d.F);
-  const int par = t & 1;
-  T *xc = d.x[par], *xn = d.x[par ^ 1];
-  T *yc = d.y[par], *yn = d.y[par ^ 1];
-  if (f.eval) enqueue_eval(off, f.infeas, f.restart_check, kEvalCheck);
-  if (f.maybe_restart) {
-    k_restart<T><<<d.ew_grid, kThreads, 0, st_>>>(d, xc, yc);
-    k_restart_fin<T><<<1, kThreads, 0, st_>>>(d, off);
-    PDLP_LAUNCH_CHECK();
-  }
-#define PDLP_STEPS(MAJ, FP)                                             \
-  {                                                                     \
-    PrimalEpi<T, MAJ, FP> pe{d, off, xc, yc, xn, T(0), T(0), T(0)};     \
-    launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                   \
-    DualEpi<T, MAJ, FP> de{d, off, yc, yn, T(0), T(0), T(0), T(0)};     \
-    launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                    \
-  }
-  if (f.major_kernel) {
-    if (f.fpe) PDLP_STEPS(true, true) else PDLP_STEPS(true, false)
-  } else {
-    if (f.fpe) PDLP_STEPS(false, true) else PDLP_STEPS(false, false)
-  }
-#undef PDLP_STEPS
-  if (f.fpe) {
-    if (f.fpe_restart_only) launch_spmv(AT_, FpeEpi<T, true>{d}, d.p_fpe, d.lp_fpe, st_);
-    else launch_spmv(AT_, FpeEpi<T, false>{d}, d.p_fpe, d.lp_fpe, st_);
-    k_fpe_fin<T><<<1, kThreads, 0, st_>>>(d, f.fpe_restart_only ? 1 : 0);
-    PDLP_LAUNCH_CHECK();
-  }
-}
-
-// kernels one iteration launches (early exits included)
-static long iteration_launches(const IterFlags &f) {
-  return 2 + (f.eval ? 3 + (f.infeas ? 4 : 0) : 0) + (f.maybe_restart ? 2 : 0) + (f.fpe ? 2 : 0);
-}
-
-template <class T>
-cudaGraphExec_t Solve<T>::chunk_graph(int t0, int t1) {
-  std::string key;
-  key.reserve((size_t)(t1 - t0) * 2 + 2);
-  key += (char)('0' + (t0 & 1));
-  for (int t = t0; t < t1; ++t) {
-    IterFlags f = iteration_flags(t, d_.F);
-    key += (char)('A' + (f.eval) + 2 * f.infeas + 4 * f.restart_check + 8 * f.maybe_restart);
-    key += (char)('A' + (f.major_kernel) + 2 * f.fpe + 4 * f.fpe_restart_only);
-  }
-  auto it = graphs_.find(key);
-  if (it != graphs_.end()) return it->second;
-  cudaGraph_t g;
-  cudaGraphExec_t e;
-  PDLP_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-  for (int t = t0; t < t1; ++t) enqueue_iteration(t, t - t0);
-  PDLP_CUDA(cudaStreamEndCapture(st_, &g));
-  PDLP_CUDA(cudaGraphInstantiate(&e, g, 0));
-  raw_graphs_.push_back(g);
-  graphs_[key] = e;
-  return e;
-}
-
-template <class T>
-void Solve<T>::run() {
-  Dev<T> &d = d_;
-  const int L = p_.termination_criteria.iteration_limit;
-  const int CH = 100;
-  auto t0 = std::chrono::steady_clock::now();
-  k_loop_start<<<1, 1, 0, st_>>>(d.ctl);
-  PDLP_LAUNCH_CHECK();
-  launches_ += 1;
-  cudaEvent_t ev[2];
-  PDLP_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
-  PDLP_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
-  int t = 0, k = 0;
-  while (t < L) {
-    if (hflag_->done) break;
-    int t1 = (int)std::min<long>((long)L, ((long)t / CH + 1) * CH);
-    cudaGraphExec_t g = chunk_graph(t, t1);
-    if (k >= 2) PDLP_CUDA(cudaEventSynchronize(ev[k & 1]));
-    if (hflag_->done) break;
-    k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, t);
-    PDLP_LAUNCH_CHECK();
-    PDLP_CUDA(cudaGraphLaunch(g, st_));
-    PDLP_CUDA(cudaEventRecord(ev[k & 1], st_));
-    for (int tt = t; tt < t1; ++tt) launches_ += iteration_launches(iteration_flags(tt, d.F));
-    launches_ += 1;
-    ++k;
-    t = t1;
-  }
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-  cudaEventDestroy(ev[0]);
-  cudaEventDestroy(ev[1]);
-  if (!hflag_->done) {
-    // iteration limit: one more evaluation at total_count = L (solver.cu:105-109)
-    k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, L);
-    enqueue_eval(0, false, false, kEvalIterLimit);
-    launches_ += 4;
-    PDLP_CUDA(cudaStreamSynchronize(st_));
-  }
-  loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-}
-
-template <class T>
-void Solve<T>::time_kernels(int reps, double *ms) {
-  Dev<T> &d = d_;
-  cudaEvent_t e0, e1;
-  PDLP_CUDA(cudaEventCreate(&e0));
-  PDLP_CUDA(cudaEventCreate(&e1));
-  auto timed = [&](auto &&launch) {
-    launch();  // warm
-    PDLP_CUDA(cudaEventRecord(e0, st_));
-    for (int i = 0; i < reps; ++i) launch();
-    PDLP_CUDA(cudaEventRecord(e1, st_));
-    PDLP_CUDA(cudaEventSynchronize(e1));
-    float t = 0;
-    PDLP_CUDA(cudaEventElapsedTime(&t, e0, e1));
-    return (double)t / reps;
-  };
-  PrimalEpi<T, false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
-  DualEpi<T, false, false> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
-  ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
-  ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
-  ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<T, false>{d}, d.p_e1, d.lp_e1, st_); });
-  ms[3] = timed([&] { launch_spmv(AT_, EvalATEpi<T, false>{d}, d.p_e2, d.lp_e2, st_); });
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-}
-
-template <class T>
-int Solve<T>::reason() const {
-  Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  return c.reason;
-}
-
-template <class T>
-int Solve<T>::total_count() const {
-  Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  return c.final_t;
-}
-
-template <class T>
-std::vector<double> Solve<T>::trace() const {
-  Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
-  std::vector<double> tr((size_t)c.trace_len * 10);
-  if (c.trace_len)
-    PDLP_CUDA(cudaMemcpy(tr.data(), d_.trace, tr.size() * 8, cudaMemcpyDeviceToHost));
-  return tr;
-}
-
-template <class T>
-void Solve<T>::result_device(double *x, double *y, double *lam) {
-  Dev<T> d = d_;
-  if (snapshot_) {  // the best evaluated iterate of the run
-    Ctl c;
-    PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
-    PDLP_CUDA(cudaStreamSynchronize(st_));
-    if (c.snap_err < INFINITY) {
-      d.xhat = d.bx;
-      d.yhat = d.by;
-      d.lam = d.bl;
-    }
-  }
-  k_unscale<T><<<grid_for((long)d.n + d.m), kThreads, 0, st_>>>(d, x, y, lam);
-  PDLP_LAUNCH_CHECK();
-}
-
-template <class T>
-Kkt Solve<T>::evaluate(const double *x, const double *y, const double *lam) {
-  Dev<T> &d = d_;
-  k_scale_point<T><<<grid_for((long)d.n + d.m), kThreads, 0, st_>>>(d, x, y, lam);
-  PDLP_LAUNCH_CHECK();
-  k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, 0);
-  enqueue_eval(0, false, false, kEvalOnly);
-  Ctl c;
-  PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-  return Kkt{c.abs_primal_res, c.rel_primal_res, c.abs_dual_res, c.rel_dual_res,
-             c.primal_obj,     c.dual_obj,       c.gap,          c.rel_gap};
-}
-
-template <class T>
-cupdlpx_result_t *Solve<T>::result() {
-  Dev<T> &d = d_;
-  const int n = d.n, m = d.m;
-  launch_spmv(AT_, ReducedCostEpi<T>{d, outl_}, nullptr, nullptr, st_);
-  result_device(outx_, outy_, nullptr);
-  launches_ += 2;
-  auto *r = (cupdlpx_result_t *)calloc(1, sizeof(cupdlpx_result_t));
-  if (!r) throw std::bad_alloc();
-  r->primal_solution = (double *)malloc(sizeof(double) * (n ? n : 1));
-  r->dual_solution = (double *)malloc(sizeof(double) * (m ? m : 1));
-  r->reduced_cost = (double *)malloc(sizeof(double) * (n ? n : 1));
-  if (!r->primal_solution || !r->dual_solution || !r->reduced_cost) {
-    free(r->primal_solution);
-    free(r->dual_solution);
-    free(r->reduced_cost);
-    free(r);
-    throw std::bad_alloc();
-  }
-  if (n) {
-    PDLP_CUDA(cudaMemcpyAsync(r->primal_solution, outx_, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
-    PDLP_CUDA(cudaMemcpyAsync(r->reduced_cost, outl_, (size_t)n * 8, cudaMemcpyDeviceToHost, st_));
-  }
-  if (m)
-    PDLP_CUDA(cudaMemcpyAsync(r->dual_solution, outy_, (size_t)m * 8, cudaMemcpyDeviceToHost, st_));
-  Ctl c;
-  PDLP_CUDA(cudaMemcpyAsync(&c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
-  PDLP_CUDA(cudaStreamSynchronize(st_));
-  r->num_variables = n;
-  r->num_constraints = m;
-  r->num_nonzeros = P_.nnz;
-  r->num_reduced_variables = n;
-  r->num_reduced_constraints = m;
-  r->num_reduced_nonzeros = P_.nnz;
-  r->total_count = c.final_t;
-  r->rescaling_time_sec = rescale_sec_;
-  r->cumulative_time_sec = c.cum_time;
-  r->presolve_time = 0.0;
-  r->presolve_status = 0;
-  r->absolute_primal_residual = c.abs_primal_res;
-  r->relative_primal_residual = c.rel_primal_res;
-  r->absolute_dual_residual = c.abs_dual_res;
-  r->relative_dual_residual = c.rel_dual_res;
-  r->primal_objective_value = c.primal_obj;
-  r->dual_objective_value = c.dual_obj;
-  r->objective_gap = c.gap;
-  r->relative_objective_gap = c.rel_gap;
-  r->max_primal_ray_infeasibility = c.max_primal_ray_inf;
-  r->max_dual_ray_infeasibility = c.max_dual_ray_inf;
-  r->primal_ray_linear_objective = c.primal_ray_obj;
-  r->dual_ray_objective = c.dual_ray_obj;
-  r->termination_reason = (termination_reason_t)c.reason;
-  r->feasibility_polishing_time = 0.0;
-  r->feasibility_iteration = 0;
-  return r;
-}
-
-template class Solve<double>;
-template class Solve<float>;
+template class Solve<double, double>;
 
 }  // namespace pdlp

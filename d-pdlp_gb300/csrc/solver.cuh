@@ -60,7 +60,7 @@ struct Dev {
   // LP at (sx + x, sy + y), from its objective and finite bounds
   int shifted;
   const double *sx, *sy, *oc, *olcf, *oucf;
-  double oc0;
+  double oc0, sdp_inv, sdd_inv;  // 1/Delta_p, 1/Delta_d of the correction
   // best-iterate snapshot (refinement rounds): copies of x_hat, y_hat, lam
   T *bx, *by, *bl;
   // reduction partials, one buffer per launch site
@@ -129,6 +129,7 @@ struct DevProblem {
   const double *shift_x = nullptr, *shift_y = nullptr, *orig_c = nullptr;
   const double *orig_lcf = nullptr, *orig_ucf = nullptr;
   double orig_c0 = 0;
+  double delta_p = 1.0, delta_d = 1.0;  // correction scalings (x - xbar) Delta_p, ...
   void *arena = nullptr;  // owned device memory (null for a view)
   size_t bytes = 0;
   ~DevProblem();
@@ -142,13 +143,24 @@ struct Kkt {
   double abs_p, rel_p, abs_d, rel_d, pobj, dobj, gap, rel_gap;
 };
 
-// One single-LP solve on one stream; T = double (FP64 path) or float (FP32
-// path with FP64 reductions).
-template <class T>
+// One single-LP solve on one stream.  T is the type of the iterates and of
+// the per-element update arithmetic, M the type of the matrix values and of
+// the SpMV products and accumulation:
+//   <double, double>  FP64 path (the reference's arithmetic)
+//   <float,  float>   FP32 path (iterates and SpMVs in FP32)
+//   <double, float>   FP32 matrix and SpMVs, FP64 iterates and updates
+// Reductions, control scalars, rescaling and unscaling are FP64 in all three.
+template <class T, class M = T>
 class Solve {
  public:
   Solve(const pdhg_parameters_t &params, cudaStream_t stream, const DevProblem &prob,
         int trace_cap = 0);
+  // Use these bound / objective scalings instead of the reference rule
+  // (before prepare()).
+  void set_fixed_scaling(double cb, double ob) {
+    fixed_cb_ = cb;
+    fixed_ob_ = ob;
+  }
   // Enable the stall rule (before run()).
   void set_stall_rule(int min_iters, double frac) {
     d_.stall_min = min_iters;
@@ -194,7 +206,7 @@ class Solve {
   int reason() const;
   int total_count() const;
   const Dev<T> &dev() const { return d_; }
-  const DevCsrT<T> &A() const { return A_; }
+  const DevCsrT<M> &A() const { return A_; }
   const DevCsr &A64() const { return A64_; }
   // scaled FP64 vectors (valid after prepare)
   const double *c64() const { return c64_; }
@@ -216,7 +228,7 @@ class Solve {
   Dev<T> d_{};
   PowDev pw_{};
   DevCsr A64_, AT64_;   // FP64 scaled working copies (rescaling, power method)
-  DevCsrT<T> A_, AT_;   // iteration matrices (== A64_/AT64_ for T = double)
+  DevCsrT<M> A_, AT_;   // iteration matrices (== A64_/AT64_ for M = double)
   double *c64_ = nullptr, *lv64_ = nullptr, *uv64_ = nullptr, *lc64_ = nullptr,
          *uc64_ = nullptr;
   double *outx_ = nullptr, *outy_ = nullptr, *outl_ = nullptr;  // FP64 results
@@ -231,14 +243,20 @@ class Solve {
   long launches_ = 0;
   bool snapshot_ = false;
   void *snap_mem_ = nullptr;
+  double fixed_cb_ = 0.0, fixed_ob_ = 0.0;
 };
+
+extern template class Solve<double, double>;
+extern template class Solve<float, float>;
+extern template class Solve<double, float>;
 
 // GPU rescaling (precond.cu): Ruiz, Pock-Chambolle, bound/objective scaling
 // on the device copies of A, A^T, c, bounds.  Fills Dr, Dc, cb, ob.
 void gpu_rescale(const pdhg_parameters_t &p, DevCsr &A, DevCsr &AT, double *c,
                  double *lv, double *uv, double *lc, double *uc, double *Dr,
                  double *Dc, double *cb, double *ob, double *tmp_n, double *tmp_m,
-                 double *part, cudaStream_t st);
+                 double *part, cudaStream_t st, double fixed_cb = 0.0,
+                 double fixed_ob = 0.0);
 
 // Stable transpose of a host CSR (rows of A^T ordered by original row).
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
@@ -249,6 +267,7 @@ void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax
 struct RefineOptions {
   int max_rounds = 8;       // outer refinement rounds
   double inner_eps = 0.0;   // tolerance of each FP32 solve (0: automatic)
+  bool fp64_iterates = false;  // rounds run Solve<double, float> instead of <float, float>
 };
 
 struct RefineReport {

@@ -178,7 +178,7 @@ class SolveInfo(C.Structure):
     ]
 
 
-PRECISION_FP64, PRECISION_FP32_REFINE = 0, 1
+PRECISION_FP64, PRECISION_FP32_REFINE, PRECISION_FP32_MATRIX = 0, 1, 2
 
 
 class Options(C.Structure):

@@ -41,9 +41,14 @@ typedef struct {
  *   refinement re-centre the LP at the FP64 point until the FP64 KKT of the
  *   original problem meets the requested tolerances.
  * The drop-in solve_lp_problem() uses FP64 unless the environment variable
- * PDLP_PRECISION is "fp32". */
+ * PDLP_PRECISION is "fp32" (FP32_REFINE) or "fp32m" (FP32_MATRIX). */
 #define PDLP_PRECISION_FP64 0
 #define PDLP_PRECISION_FP32_REFINE 1
+/* FP32_MATRIX: matrix values, SpMV products and their accumulation in FP32;
+ * iterates and the per-element updates in FP64 (no FP32 absorption floor);
+ * reductions in FP64.  Same refinement rounds as FP32_REFINE when the FP64
+ * KKT of the original LP misses the tolerances. */
+#define PDLP_PRECISION_FP32_MATRIX 2
 
 typedef struct {
   int precision;          /* PDLP_PRECISION_* */
