@@ -369,9 +369,9 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-4)
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default="fp32m",
-                    help="fp32: FP32 iterates + FP64 refinement; fp32m (default): FP32 matrix "
-                         "and SpMVs with FP64 iterates + FP64 refinement; fp64: plain FP64")
+    ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default="fp64",
+                    help="fp32: FP32 iterates + FP64 refinement; fp32m: FP32 matrix "
+                         "and SpMVs with FP64 iterates + FP64 refinement; fp64 (default): plain FP64")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed FP64 solves reported beside an FP32 run (0: skip)")
     args = ap.parse_args()

@@ -214,17 +214,18 @@ __global__ void __launch_bounds__(kThreads)
   } else if (b.y >= 0) {
     const int r0 = b.x;
     if (R == 1) {
+      // one long light row: lane chains in A, cross-lane sums in FP64
       A s = A(0);
       for (int i = threadIdx.x; i < len; i += kThreads)
         s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
-      A v = warp_sum(s);
+      double v = warp_sum((double)s);
       int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      if (lane == 0) red[wid] = (double)v;
+      if (lane == 0) red[wid] = v;
       __syncthreads();
       if (threadIdx.x == 0) {
-        A tot = A(0);
-        for (int w = 0; w < kThreads / 32; ++w) tot += (A)red[w];
-        epi.row(r0, tot, acc);
+        double tot = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) tot += red[w];
+        epi.row(r0, (A)tot, acc);
       }
     } else if (R > 1) {
       // few long rows: a group of G lanes per row
@@ -237,23 +238,25 @@ __global__ void __launch_bounds__(kThreads)
         int beg = soff[grp], end = soff[grp + 1];
         for (int i = beg + li; i < end; i += G) s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
       }
-      for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (li == 0 && grp < R) epi.row(r0 + grp, s, acc);
+      double sd = s;  // cross-lane sums in FP64
+      for (int o = G >> 1; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+      if (li == 0 && grp < R) epi.row(r0 + grp, (A)sd, acc);
     }
   } else {
-    // chunk of a long row
+    // chunk of a long row: lane chains in A, every sum across lanes, warps
+    // and chunks in FP64 (rows of up to ~10^5 terms with cancellation)
     A s = A(0);
     for (int i = threadIdx.x; i < len; i += kThreads)
       s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
-    A v = warp_sum(s);
+    double v = warp_sum((double)s);
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = (double)v;
+    if (lane == 0) red[wid] = v;
     __syncthreads();
     const int lid = -b.y - 1;
     if (threadIdx.x == 0) {
-      A tot = A(0);
-      for (int w = 0; w < kThreads / 32; ++w) tot += (A)red[w];
-      plan.lsum[blockIdx.x] = (double)tot;
+      double tot = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) tot += red[w];
+      plan.lsum[blockIdx.x] = tot;
       __threadfence();
       unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
       s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
@@ -262,12 +265,12 @@ __global__ void __launch_bounds__(kThreads)
     if (s_last && threadIdx.x == 0) {
       __threadfence();
       const int2 L = plan.lrow[lid];
-      A tot = A(0);
-      for (int c = 0; c < L.y; ++c) tot += (A)__ldcg(plan.lsum + L.x + c);
+      double tot = 0.0;
+      for (int c = 0; c < L.y; ++c) tot += __ldcg(plan.lsum + L.x + c);
       double lacc[NF > 0 ? NF : 1];
 #pragma unroll
       for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
-      epi.row(b.x, tot, lacc);
+      epi.row(b.x, (A)tot, lacc);
       if constexpr (NF > 0) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
