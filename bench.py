@@ -56,9 +56,9 @@ DEFAULT_WORKLOAD = "powerlaw_m1M_n2M_nnz20M_seed1"
 # evaluation trace matches the GPU's in the parity tests), so the reference
 # arm extrapolates its bounded samples with them.
 REFERENCE_COUNTS = {
-    "powerlaw_m1M_n2M_nnz20M_seed1": {"iterations": None, "power_iterations": None},
-    "transport_2000x5000_seed2": {"iterations": None, "power_iterations": None},
-    "random_m2k_n5k_nnz20k_seed0": {"iterations": 2800, "power_iterations": None},
+    "powerlaw_m1M_n2M_nnz20M_seed1": {"iterations": 51400, "power_iterations": 226},
+    "transport_2000x5000_seed2": {"iterations": 16800, "power_iterations": 22},
+    "random_m2k_n5k_nnz20k_seed0": {"iterations": 2800, "power_iterations": 78},
 }
 
 
