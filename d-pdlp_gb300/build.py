@@ -21,6 +21,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcupdlpx_gb300.so")
 
 SOURCES = ["solver.cu", "solver_f32.cu", "solver_mix.cu", "refine.cu", "precond.cu", "hooks.cu",
+           "noalloc.cu",
            "api.cpp", "lpgen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

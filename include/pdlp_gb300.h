@@ -160,6 +160,39 @@ int pdlp_gpu_power_method(const lp_problem_t *prob,
                           const pdhg_parameters_t *params, double *sigma_max,
                           int *iterations);
 
+/* ---- SpMV that allocates nothing ---------------------------------------
+ * No counterpart in the reference: an addition of this library for callers
+ * that cannot call cudaMalloc -- a host application whose own pool
+ * allocator has already reserved the device memory (a further cudaMalloc
+ * fails or breaks its accounting), or a latency-critical loop that must not
+ * take the device-wide synchronisation that cudaMalloc / cudaFree imply.
+ *
+ * y = A x for a CSR matrix (rows x cols, nnz non-zeros) with row_ptr,
+ * col_ind, vals, x and y all in DEVICE memory owned by the caller; stream is
+ * a cudaStream_t (NULL: the legacy default stream).  The call returns after
+ * the product is complete on that stream.  Its only scratch (per-tile
+ * partial sums of rows that cross 2048-non-zero tiles, and an error flag) is
+ * a 1.3 MB array in device global memory that each GPU loading this library
+ * holds until the process exits; no cudaMalloc, cudaFree or allocating
+ * library routine is called.
+ *
+ * Limits and sharing: nnz may be at most PDLP_NOALLOC_MAX_TILES * 2048
+ * (134,217,728); larger inputs return -3 without launching.  All calls share
+ * the one scratch array per device, so calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * The first call on each device looks up the array's device address with
+ * that device current; make that first call before any stream capture.
+ *
+ * Returns 0 on success; -1 bad arguments, -2 CUDA error, -3 size above the
+ * limit, -4 malformed CSR (row pointers or column indices, detected on the
+ * device; y is then unspecified).  pdlp_spmv_noalloc_error() gives the
+ * message of the calling thread's last failure. */
+#define PDLP_NOALLOC_MAX_TILES 65536
+int pdlp_spmv_noalloc(int rows, int cols, int nnz, const int *row_ptr,
+                      const int *col_ind, const double *vals, const double *x,
+                      double *y, void *stream);
+const char *pdlp_spmv_noalloc_error(void);
+
 #ifdef __cplusplus
 }
 #endif
