@@ -67,6 +67,26 @@ def rank_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def visible_device_for_rank(local: int, visible: str | None) -> str:
+    """The one GPU a replica rank uses: entry `local` of CUDA_VISIBLE_DEVICES
+    (or of 0..63 when unset); the solver library then sees it as device 0."""
+    devs = visible.split(",") if visible else [str(i) for i in range(64)]
+    return devs[local]
+
+
+def max_over_ranks(values: list[float]) -> list[float]:
+    """Element-wise max over all ranks of the default process group (NCCL on
+    GPUs, gloo on CPU); returns `values` unchanged without a process group."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return list(values)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(values, dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 def make_problem(cp, name):
     w = WORKLOADS[name]
     return cp.Problem.generated(w["kind"], *w["args"])
@@ -246,15 +266,7 @@ def run_ours(args, cp, rank, world, local):
                     "us_per_iteration": round(f_last.info["loop_seconds"] /
                                               max(1, f_last.result["total_count"]) * 1e6, 2)}
     clocks = clk.summary()
-    value = statistics.mean(dev_s)
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([value, statistics.mean(e2e_s)], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        value, e2e_mean = float(t[0]), float(t[1])
-    else:
-        e2e_mean = statistics.mean(e2e_s)
+    value, e2e_mean = max_over_ranks([statistics.mean(dev_s), statistics.mean(e2e_s)])
     r = last.result
     ms = dp.time_kernels(params, reps=args.kernel_reps, precision=prec)
     pb, db = kernel_bytes(m, n, nnz, 8)
@@ -380,9 +392,8 @@ def main():
     rank, world, local = rank_info()
     if world > 1:
         # one GPU per rank: the solver library uses device 0 of what it sees
-        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
-        devs = vis.split(",") if vis else [str(i) for i in range(64)]
-        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local]
+        os.environ["CUDA_VISIBLE_DEVICES"] = visible_device_for_rank(
+            local, os.environ.get("CUDA_VISIBLE_DEVICES"))
     import cupdlpx as cp
     if args.impl == "reference":
         if rank == 0:

@@ -277,6 +277,44 @@ double power_method(const Csr &A, const Csr &AT, const vec &v0, int max_iter,
   return std::sqrt(sigma_sq);
 }
 
+// ---------------------------------------------------------- scalar criteria
+// reference src/utils.cu:214-263 (optimality, primal / dual infeasibility,
+// iteration and time limits, in that order of precedence)
+extern "C" int oracle_termination_decision(const termination_criteria_t *tc, double rel_p,
+                                           double rel_d, double rel_gap, double dray_obj,
+                                           double max_dray, double pray_obj, double max_pray,
+                                           int total, double cum_time) {
+  if (rel_d < tc->eps_feasible_relative && rel_p < tc->eps_feasible_relative &&
+      rel_gap < tc->eps_optimal_relative)
+    return TERMINATION_REASON_OPTIMAL;
+  if (dray_obj > 0.0 && max_dray / dray_obj <= tc->eps_infeasible)
+    return TERMINATION_REASON_PRIMAL_INFEASIBLE;
+  if (pray_obj < 0.0 && max_pray / (-pray_obj) <= tc->eps_infeasible)
+    return TERMINATION_REASON_DUAL_INFEASIBLE;
+  if (total >= tc->iteration_limit) return TERMINATION_REASON_ITERATION_LIMIT;
+  if (cum_time >= tc->time_sec_limit) return TERMINATION_REASON_TIME_LIMIT;
+  return TERMINATION_REASON_UNSPECIFIED;
+}
+
+// reference src/utils.cu:265-293: restart at the first major evaluation,
+// then on sufficient decay, on necessary decay with no progress since the
+// last trial, or when the inner count passes the artificial threshold;
+// *last_fpe becomes fpe
+extern "C" int oracle_restart_decision(const restart_parameters_t *rp, int F, int total,
+                                       int inner, double fpe, double init_fpe,
+                                       double *last_fpe) {
+  bool r = false;
+  if (total == F) {
+    r = true;
+  } else if (total > F) {
+    if (fpe <= rp->sufficient_reduction_for_restart * init_fpe) r = true;
+    if (fpe <= rp->necessary_reduction_for_restart * init_fpe && fpe > *last_fpe) r = true;
+    if (inner >= rp->artificial_restart_threshold * total) r = true;
+  }
+  *last_fpe = fpe;
+  return r ? 1 : 0;
+}
+
 // ------------------------------------------------------------------- solver
 struct Solver {
   const pdhg_parameters_t &prm;
@@ -442,46 +480,15 @@ struct Solver {
     }
   }
 
-  // reference src/utils.cu:239-263
   void check_termination() {
-    const auto &tc = prm.termination_criteria;
-    if (rel_d < tc.eps_feasible_relative && rel_p < tc.eps_feasible_relative &&
-        rel_gap < tc.eps_optimal_relative) {
-      reason = TERMINATION_REASON_OPTIMAL;
-      return;
-    }
-    if (dray_obj > 0.0 && max_dray / dray_obj <= tc.eps_infeasible) {
-      reason = TERMINATION_REASON_PRIMAL_INFEASIBLE;
-      return;
-    }
-    if (pray_obj < 0.0 && max_pray / (-pray_obj) <= tc.eps_infeasible) {
-      reason = TERMINATION_REASON_DUAL_INFEASIBLE;
-      return;
-    }
-    if (total >= tc.iteration_limit) {
-      reason = TERMINATION_REASON_ITERATION_LIMIT;
-      return;
-    }
-    if (cum_time >= tc.time_sec_limit) {
-      reason = TERMINATION_REASON_TIME_LIMIT;
-      return;
-    }
+    int r = oracle_termination_decision(&prm.termination_criteria, rel_p, rel_d, rel_gap,
+                                        dray_obj, max_dray, pray_obj, max_pray, total, cum_time);
+    if (r != TERMINATION_REASON_UNSPECIFIED) reason = (termination_reason_t)r;
   }
 
-  // reference src/utils.cu:265-293
   bool should_restart() {
-    const auto &rp = prm.restart_params;
-    int F = prm.termination_evaluation_frequency;
-    bool r = false;
-    if (total == F) {
-      r = true;
-    } else if (total > F) {
-      if (fpe <= rp.sufficient_reduction_for_restart * init_fpe) r = true;
-      if (fpe <= rp.necessary_reduction_for_restart * init_fpe && fpe > last_fpe) r = true;
-      if (inner >= rp.artificial_restart_threshold * total) r = true;
-    }
-    last_fpe = fpe;
-    return r;
+    return oracle_restart_decision(&prm.restart_params, prm.termination_evaluation_frequency,
+                                   total, inner, fpe, init_fpe, &last_fpe) != 0;
   }
 
   // reference src/pdlp_core_op.cu:577-636

@@ -98,6 +98,19 @@ void oracle_session_free(oracle_session_t *s);
 /* Evaluation cadence (reference src/utils.cu:492-501). */
 int oracle_print_frequency(int iter);
 
+/* Termination reason for one evaluation's scalars (reference
+ * src/utils.cu:214-263); TERMINATION_REASON_UNSPECIFIED when none holds. */
+int oracle_termination_decision(const termination_criteria_t *tc, double rel_p,
+                                double rel_d, double rel_gap, double dray_obj,
+                                double max_dray, double pray_obj, double max_pray,
+                                int total, double cum_time);
+
+/* Adaptive restart test (reference src/utils.cu:265-293); updates
+ * *last_fpe as the reference updates last_trial_fixed_point_error. */
+int oracle_restart_decision(const restart_parameters_t *rp, int F, int total,
+                            int inner, double fpe, double init_fpe,
+                            double *last_fpe);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,7 +7,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "d-pdlp_gb300")
-for p in (PKG, os.path.join(ROOT, "tests")):
+for p in (PKG, os.path.join(ROOT, "tests"), os.path.join(ROOT, "tests", "golden")):
     if p not in sys.path:
         sys.path.insert(0, p)
 os.environ.setdefault("PDLP_QUIET", "1")  # no per-solve summary in test logs
@@ -20,6 +20,9 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def lib():
     import cupdlpx
+    if not os.path.exists(cupdlpx.LIB_PATH):
+        import build  # compiles the library (nvcc cross-compiles without a GPU)
+        build.build()
     return cupdlpx.lib()
 
 
