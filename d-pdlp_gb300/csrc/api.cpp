@@ -278,6 +278,9 @@ cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &
     info->graphs = s.graph_count();
     info->kernel_launches = s.kernel_launches();
     info->precision = PDLP_PRECISION_FP64;
+    info->primal_step_ms = s.live_primal_ms();
+    info->dual_step_ms = s.live_dual_ms();
+    info->timed_chunks = s.live_samples();
   }
   return r;
 }
@@ -312,6 +315,12 @@ cupdlpx_result_t *run_refined(const pdlp::DevProblem &P, const pdhg_parameters_t
     info->power_iterations = rep.power_iterations;
     info->sigma_max = rep.sigma_max;
     info->precision = o.precision;
+    info->timed_chunks = rep.timed_chunks;
+    info->fp64_finish = rep.fp64_finish ? 1 : 0;
+    if (rep.timed_chunks > 0) {
+      info->primal_step_ms = rep.timed_primal_ms_sum / rep.timed_chunks;
+      info->dual_step_ms = rep.timed_dual_ms_sum / rep.timed_chunks;
+    }
   }
   return r;
 }

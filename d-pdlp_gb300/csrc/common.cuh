@@ -112,6 +112,26 @@ __device__ __forceinline__ T warp_sum(T v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// max(lo, min(t, hi)), the projection onto [lo, hi] in the reference's
+// operand order (a crossed interval yields lo).  For doubles it compares
+// order-preserving integer keys -- for IEEE values, flipping the magnitude
+// bits of negatives makes signed 64-bit order equal numeric order (-0 sorts
+// below +0) -- so the projection issues on the integer pipe instead of
+// GB300's FP64 pipe, where min/max cost a full FP64 issue slot each.
+__device__ __forceinline__ long long order_key(double v) {
+  long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double clamp_to(double t, double lo, double hi) {
+  long long kt = order_key(t), kh = order_key(hi);
+  double r = kt > kh ? hi : t;
+  long long kr = kt > kh ? kh : kt;
+  return kr < order_key(lo) ? lo : r;
+}
+__device__ __forceinline__ float clamp_to(float t, float lo, float hi) {
+  return fmaxf(lo, fminf(t, hi));
+}
+
 template <class T>
 __device__ __forceinline__ T warp_max(T v) {
 #pragma unroll

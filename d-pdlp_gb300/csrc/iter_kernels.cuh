@@ -28,8 +28,10 @@ __device__ __forceinline__ void halpern_weight(const Ctl *c, int off, double *sc
 }
 
 // primal step: x_hat = proj(x - tau (c - A^T y)), x_ref = 2 x_hat - x, Halpern
-// (reference pdlp_core_op.cu:393-418, :445-462, :495-526)
-template <class T, class M, bool MAJOR, bool FPE>
+// (reference pdlp_core_op.cu:393-418, :445-462, :495-526).  RHO1: the
+// reflection coefficient is 1 (the default), so the reflected point is x_ref
+// itself.
+template <class T, class M, bool MAJOR, bool FPE, bool RHO1>
 struct PrimalEpi {
   using val_t = M;
   using acc_t = M;
@@ -56,7 +58,7 @@ struct PrimalEpi {
     T s = (T)sm;
     T xc = xcur[j];
     T t = xc - tau * (d.c[j] - s);
-    T xh = fmax(d.lv[j], fmin(t, d.uv[j]));
+    T xh = clamp_to(t, d.lv[j], d.uv[j]);
     if (MAJOR) {
       d.xhat[j] = xh;
       d.lam[j] = (xh - t) / tau;
@@ -68,14 +70,14 @@ struct PrimalEpi {
       d.dx[j] = dd;
       acc[0] += (double)dd * (double)dd;
     }
-    T refl = d.rho_is_one ? xr : (T)d.rho * xr + (T)d.one_minus_rho * xc;
+    T refl = RHO1 ? xr : (T)d.rho * xr + (T)d.one_minus_rho * xc;
     xnext[j] = w * refl + omw * d.x0[j];
   }
 };
 
 // dual step: t = y/sigma - A x_ref, y_hat = sigma (t - proj(t)), Halpern
 // (reference pdlp_core_op.cu:420-443, :528-557)
-template <class T, class M, bool MAJOR, bool FPE>
+template <class T, class M, bool MAJOR, bool FPE, bool RHO1>
 struct DualEpi {
   using val_t = M;
   using acc_t = M;
@@ -105,7 +107,7 @@ struct DualEpi {
     // the reference divides by sigma; one reciprocal per launch instead
     // (at most 1 ulp apart; an FP64 division costs ~10 FP64 issue slots)
     T t = yc * inv_sigma - s;
-    T tp = fmax(-d.uc[i], fmin(t, -d.lc[i]));
+    T tp = clamp_to(t, -d.uc[i], -d.lc[i]);
     T yh = (t - tp) * sigma;
     if (MAJOR) d.yhat[i] = yh;
     T yr = T(2) * yh - yc;
@@ -114,7 +116,7 @@ struct DualEpi {
       d.dy[i] = dd;
       acc[0] += (double)dd * (double)dd;
     }
-    T refl = d.rho_is_one ? yr : (T)d.rho * yr + (T)d.one_minus_rho * yc;
+    T refl = RHO1 ? yr : (T)d.rho * yr + (T)d.one_minus_rho * yc;
     ynext[i] = w * refl + omw * d.y0[i];
   }
 };

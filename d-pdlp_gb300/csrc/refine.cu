@@ -277,6 +277,9 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
       iters += s.total_count();
       launches += s.kernel_launches();
       rep.rounds = round + 1;
+      rep.timed_primal_ms_sum += s.live_primal_ms() * s.live_samples();
+      rep.timed_dual_ms_sum += s.live_dual_ms() * s.live_samples();
+      rep.timed_chunks += s.live_samples();
       if (r == TERMINATION_REASON_PRIMAL_INFEASIBLE || r == TERMINATION_REASON_DUAL_INFEASIBLE) {
         // infeasibility certificates come from the first round's rays
         ray_result = s.result();
@@ -305,6 +308,9 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
         launches += 2;
         return true;
       }
+      // a correction that gains less than 10x has met the FP32 floor of its
+      // own solve: keep its point, but hand over to the FP64 finish
+      const bool weak = round > 0 && err > 0.1 * best_err;
       best_err = err;
       kkt = k;
       if (err < 1.0) {
@@ -316,7 +322,7 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
         reason = r == TERMINATION_REASON_TIME_LIMIT ? r : TERMINATION_REASON_ITERATION_LIMIT;
         return true;
       }
-      return false;
+      return weak;
     };
     if (opt.fp64_iterates) {
       Solve<double, float> s(pi, st, R, 0);
@@ -328,6 +334,68 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
     if (stop) break;
   }
   (void)linf;
+  // FP64 finish: when a correction round could not improve the point, or the
+  // rounds ran out, FP64 PDHG (the reference's arithmetic) continues from the
+  // best FP64 point with round 0's step size and primal weight, so the
+  // requested tolerance stays reachable whatever floor FP32 met.
+  const double left_sec = params.termination_criteria.time_sec_limit -
+                          std::chrono::duration<double>(std::chrono::steady_clock::now() - t0)
+                              .count();
+  if (!ray_result && reason != TERMINATION_REASON_OPTIMAL &&
+      reason != TERMINATION_REASON_TIME_LIMIT && iters < limit && left_sec > 0.0) {
+    DevProblem W;  // a view of P warm-started at the FP64 point
+    W.m = m;
+    W.n = n;
+    W.nnz = nnz;
+    W.tile = P.tile;
+    W.A = P.A;
+    W.AT = P.AT;
+    W.c = P.c;
+    W.lv = P.lv;
+    W.uv = P.uv;
+    W.lc = P.lc;
+    W.uc = P.uc;
+    W.cnorm_l2 = P.cnorm_l2;
+    W.cnorm_linf = P.cnorm_linf;
+    W.bnorm_l2 = P.bnorm_l2;
+    W.bnorm_linf = P.bnorm_linf;
+    W.c0 = P.c0;
+    W.xs = xbar;
+    W.ys = ybar;
+    pdhg_parameters_t pf = params;
+    pf.termination_criteria.iteration_limit = (int)(limit - iters);
+    pf.termination_criteria.time_sec_limit = left_sec;
+    Solve<double> s(pf, st, W, 0);
+    s.prepare();
+    s.init_step(sigma, omega0);
+    s.run();
+    iters += s.total_count();
+    launches += s.kernel_launches();
+    const int r = s.reason();
+    s.result_device(xbar, ybar, lz);
+    launch_spmv(AT, RcEpi{ybar, P.c, P.lv, P.uv, rc, lam}, nullptr, nullptr, st);
+    launches += 1;
+    Kkt k = ev.evaluate(xbar, ybar, lam);
+    double err = fmax(k.rel_p / eps_feas, fmax(k.rel_d / eps_feas, k.rel_gap / eps_opt));
+    if (err >= 1.0) {
+      // the solve's own dual slack, when the projected reduced cost is worse
+      Kkt k2 = ev.evaluate(xbar, ybar, lz);
+      double err2 = fmax(k2.rel_p / eps_feas, fmax(k2.rel_d / eps_feas, k2.rel_gap / eps_opt));
+      if (err2 < err) {
+        k = k2;
+        err = err2;
+        PDLP_CUDA(cudaMemcpyAsync(lam, lz, vn * 8, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+    launches += 8;
+    kkt = k;
+    rep.rounds += 1;
+    rep.fp64_finish = true;
+    reason = err < 1.0 || r == TERMINATION_REASON_OPTIMAL ? TERMINATION_REASON_OPTIMAL : r;
+    if (params.verbose)
+      printf("FP64 finish: %d iterations (reason %d) -> FP64 rel primal %.3e rel dual %.3e "
+             "rel gap %.3e\n", s.total_count(), r, k.rel_p, k.rel_d, k.rel_gap);
+  }
   double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   rep.inner_iterations = iters;
   rep.kernel_launches = launches;

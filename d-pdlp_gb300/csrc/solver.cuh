@@ -7,6 +7,7 @@
 // unscaling run in FP64.
 #pragma once
 
+#include <array>
 #include <map>
 #include <memory>
 #include <string>
@@ -194,6 +195,14 @@ class Solve {
   // ms[2] evaluation over A, ms[3] evaluation over A^T.
   void time_kernels(int reps, double *ms);
 
+  // In-loop timing of the plain iteration kernels: in every 100-iteration
+  // chunk one ordinary iteration's primal and dual launches are bracketed by
+  // CUDA events captured into the chunk graph; the averages cover the chunks
+  // that ran before termination (after run()).
+  double live_primal_ms() const;
+  double live_dual_ms() const;
+  int live_samples() const;
+
   // diagnostics
   int power_iterations() const { return pm_iters_; }
   double sigma_max() const { return sigma_max_; }
@@ -217,9 +226,11 @@ class Solve {
 
  private:
   void alloc();
-  void enqueue_iteration(int t, int off);
+  void enqueue_iteration(int t, int off, bool timed = false);
   void enqueue_eval(int off, bool infeas, bool restart_check, int mode);
   cudaGraphExec_t chunk_graph(int t0, int t1);
+  int timed_iteration(int t0, int t1) const;
+  void read_timing(int slot);
   void power_method();
 
   pdhg_parameters_t p_;
@@ -236,6 +247,17 @@ class Solve {
   HostFlag *hflag_ = nullptr;
   int trace_cap_ = 0;
   std::map<std::string, cudaGraphExec_t> graphs_;
+  // timing: the 3 event-record nodes of each timed chunk graph, pointed at
+  // the events of the chunk's parity slot before each launch
+  std::map<cudaGraphExec_t, std::array<cudaGraphNode_t, 3>> tnodes_;
+  cudaEvent_t tev_[2][3] = {};
+  int tpending_[2] = {-1, -1};  // timed iteration recorded in each slot
+  struct TimingSample {
+    int t;
+    float primal_ms, dual_ms;
+  };
+  std::vector<TimingSample> tsamples_;
+  int final_count_ = 0;
   std::vector<cudaGraph_t> raw_graphs_;
   int pm_iters_ = 0;
   double sigma_max_ = 0.0;
@@ -278,6 +300,10 @@ struct RefineReport {
   long kernel_launches = 0;
   double seconds = 0.0;
   Kkt kkt{};
+  bool fp64_finish = false;  // the last round ran FP64 PDHG from the best point
+  // in-loop kernel timing summed over the FP32 rounds (ms x chunks)
+  double timed_primal_ms_sum = 0.0, timed_dual_ms_sum = 0.0;
+  int timed_chunks = 0;
 };
 
 // FP32 PDHG with FP64 iterative refinement on a resident problem; returns

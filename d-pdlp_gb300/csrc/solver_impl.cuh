@@ -26,6 +26,8 @@
 #include <chrono>
 #include <random>
 
+#include <type_traits>
+
 #include "iter_kernels.cuh"
 
 namespace pdlp {
@@ -415,6 +417,9 @@ Solve<T, M>::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const D
 template <class T, class M>
 Solve<T, M>::~Solve() {
   if (snap_mem_) cudaFree(snap_mem_);
+  for (auto &slot : tev_)
+    for (auto ev : slot)
+      if (ev) cudaEventDestroy(ev);
   for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
   for (auto g : raw_graphs_) cudaGraphDestroy(g);
   if (arena_) cudaFree(arena_);
@@ -759,7 +764,7 @@ double Solve<T, M>::primal_weight() const {
 }
 
 template <class T, class M>
-void Solve<T, M>::enqueue_iteration(int t, int off) {
+void Solve<T, M>::enqueue_iteration(int t, int off, bool timed) {
   Dev<T> &d = d_;
   IterFlags f = iteration_flags(t, d.F);
   const int par = t & 1;
@@ -771,19 +776,41 @@ void Solve<T, M>::enqueue_iteration(int t, int off) {
     k_restart_fin<T><<<1, kThreads, 0, st_>>>(d, off);
     PDLP_LAUNCH_CHECK();
   }
-#define PDLP_STEPS(MAJ, FP)                                             \
-  {                                                                     \
-    PrimalEpi<T, M, MAJ, FP> pe{d, off, xc, yc, xn, T(0), T(0), T(0)};     \
-    launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                   \
-    DualEpi<T, M, MAJ, FP> de{d, off, yc, yn, T(0), T(0), T(0), T(0)};     \
-    launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                    \
+#define PDLP_STEPS_R(MAJ, FP, R1)                                           \
+  {                                                                         \
+    PrimalEpi<T, M, MAJ, FP, R1> pe{d, off, xc, yc, xn, T(0), T(0), T(0)};     \
+    launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);                       \
+    DualEpi<T, M, MAJ, FP, R1> de{d, off, yc, yn, T(0), T(0), T(0), T(0)};     \
+    launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);                        \
+  }
+#define PDLP_STEPS(MAJ, FP)                                                 \
+  {                                                                         \
+    if (d.rho_is_one) PDLP_STEPS_R(MAJ, FP, true) else PDLP_STEPS_R(MAJ, FP, false) \
   }
   if (f.major_kernel) {
     if (f.fpe) PDLP_STEPS(true, true) else PDLP_STEPS(true, false)
+  } else if (f.fpe) {
+    PDLP_STEPS(false, true)
+  } else if (timed) {
+    // ordinary iteration sampled for the in-loop kernel timing; external
+    // records become event-record nodes of the captured graph
+    auto steps = [&](auto r1) {
+      constexpr bool R1 = decltype(r1)::value;
+      PrimalEpi<T, M, false, false, R1> pe{d, off, xc, yc, xn, T(0), T(0), T(0)};
+      DualEpi<T, M, false, false, R1> de{d, off, yc, yn, T(0), T(0), T(0), T(0)};
+      PDLP_CUDA(cudaEventRecordWithFlags(tev_[0][0], st_, cudaEventRecordExternal));
+      launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_);
+      PDLP_CUDA(cudaEventRecordWithFlags(tev_[0][1], st_, cudaEventRecordExternal));
+      launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_);
+      PDLP_CUDA(cudaEventRecordWithFlags(tev_[0][2], st_, cudaEventRecordExternal));
+    };
+    if (d.rho_is_one) steps(std::true_type{});
+    else steps(std::false_type{});
   } else {
-    if (f.fpe) PDLP_STEPS(false, true) else PDLP_STEPS(false, false)
+    PDLP_STEPS(false, false)
   }
 #undef PDLP_STEPS
+#undef PDLP_STEPS_R
   if (f.fpe) {
     if (f.fpe_restart_only) launch_spmv(AT_, FpeEpi<T, M, true>{d}, d.p_fpe, d.lp_fpe, st_);
     else launch_spmv(AT_, FpeEpi<T, M, false>{d}, d.p_fpe, d.lp_fpe, st_);
@@ -809,15 +836,89 @@ cudaGraphExec_t Solve<T, M>::chunk_graph(int t0, int t1) {
   }
   auto it = graphs_.find(key);
   if (it != graphs_.end()) return it->second;
+  const int tt = timed_iteration(t0, t1);
+  if (tt >= 0 && !tev_[0][0])
+    for (auto &slot : tev_)
+      for (auto &ev : slot) PDLP_CUDA(cudaEventCreate(&ev));
   cudaGraph_t g;
   cudaGraphExec_t e;
   PDLP_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-  for (int t = t0; t < t1; ++t) enqueue_iteration(t, t - t0);
+  for (int t = t0; t < t1; ++t) enqueue_iteration(t, t - t0, t == tt);
   PDLP_CUDA(cudaStreamEndCapture(st_, &g));
   PDLP_CUDA(cudaGraphInstantiate(&e, g, 0));
   raw_graphs_.push_back(g);
   graphs_[key] = e;
+  if (tt >= 0) {
+    // the event-record nodes, identified by the event each one records
+    size_t nn = 0;
+    PDLP_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    PDLP_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+    std::array<cudaGraphNode_t, 3> tn{};
+    int found = 0;
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType ty;
+      PDLP_CUDA(cudaGraphNodeGetType(nd, &ty));
+      if (ty != cudaGraphNodeTypeEventRecord) continue;
+      cudaEvent_t ev;
+      PDLP_CUDA(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+      for (int i = 0; i < 3; ++i)
+        if (ev == tev_[0][i]) {
+          tn[i] = nd;
+          ++found;
+        }
+    }
+    if (found == 3) tnodes_[e] = tn;
+  }
   return e;
+}
+
+// An ordinary iteration (no evaluation, restart, major or fixed-point-error
+// kernels) in the second half of the chunk, or -1.
+template <class T, class M>
+int Solve<T, M>::timed_iteration(int t0, int t1) const {
+  for (int t = t0 + (t1 - t0) / 2; t < t1; ++t) {
+    IterFlags f = iteration_flags(t, d_.F);
+    if (!f.eval && !f.maybe_restart && !f.major_kernel && !f.fpe) return t;
+  }
+  return -1;
+}
+
+template <class T, class M>
+void Solve<T, M>::read_timing(int slot) {
+  if (tpending_[slot] < 0) return;
+  float a = 0.f, b = 0.f;
+  if (cudaEventElapsedTime(&a, tev_[slot][0], tev_[slot][1]) == cudaSuccess &&
+      cudaEventElapsedTime(&b, tev_[slot][1], tev_[slot][2]) == cudaSuccess)
+    tsamples_.push_back({tpending_[slot], a, b});
+  else
+    cudaGetLastError();
+  tpending_[slot] = -1;
+}
+
+template <class T, class M>
+double Solve<T, M>::live_primal_ms() const {
+  double s = 0;
+  int k = 0;
+  for (const auto &x : tsamples_)
+    if (x.t + 10 < final_count_) s += x.primal_ms, ++k;
+  return k ? s / k : 0.0;
+}
+
+template <class T, class M>
+double Solve<T, M>::live_dual_ms() const {
+  double s = 0;
+  int k = 0;
+  for (const auto &x : tsamples_)
+    if (x.t + 10 < final_count_) s += x.dual_ms, ++k;
+  return k ? s / k : 0.0;
+}
+
+template <class T, class M>
+int Solve<T, M>::live_samples() const {
+  int k = 0;
+  for (const auto &x : tsamples_) k += x.t + 10 < final_count_;
+  return k;
 }
 
 template <class T, class M>
@@ -837,8 +938,18 @@ void Solve<T, M>::run() {
     if (hflag_->done) break;
     int t1 = (int)std::min<long>((long)L, ((long)t / CH + 1) * CH);
     cudaGraphExec_t g = chunk_graph(t, t1);
-    if (k >= 2) PDLP_CUDA(cudaEventSynchronize(ev[k & 1]));
+    const int slot = k & 1;
+    if (k >= 2) {
+      PDLP_CUDA(cudaEventSynchronize(ev[slot]));
+      read_timing(slot);  // chunk k-2 used this slot's events and has finished
+    }
     if (hflag_->done) break;
+    auto tn = tnodes_.find(g);
+    if (tn != tnodes_.end()) {
+      for (int i = 0; i < 3; ++i)
+        PDLP_CUDA(cudaGraphExecEventRecordNodeSetEvent(g, tn->second[i], tev_[slot][i]));
+      tpending_[slot] = timed_iteration(t, t1);
+    }
     k_set_tbase<<<1, 1, 0, st_>>>(d.ctl, t);
     PDLP_LAUNCH_CHECK();
     PDLP_CUDA(cudaGraphLaunch(g, st_));
@@ -849,6 +960,8 @@ void Solve<T, M>::run() {
     t = t1;
   }
   PDLP_CUDA(cudaStreamSynchronize(st_));
+  read_timing(0);
+  read_timing(1);
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   if (!hflag_->done) {
@@ -859,6 +972,7 @@ void Solve<T, M>::run() {
     PDLP_CUDA(cudaStreamSynchronize(st_));
   }
   loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  final_count_ = total_count();
 }
 
 template <class T, class M>
@@ -877,8 +991,9 @@ void Solve<T, M>::time_kernels(int reps, double *ms) {
     PDLP_CUDA(cudaEventElapsedTime(&t, e0, e1));
     return (double)t / reps;
   };
-  PrimalEpi<T, M, false, false> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
-  DualEpi<T, M, false, false> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
+  // the default reflection coefficient (1) selects the kernels of a solve
+  PrimalEpi<T, M, false, false, true> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
+  DualEpi<T, M, false, false, true> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
   ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
   ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
   ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<T, M, false>{d}, d.p_e1, d.lp_e1, st_); });

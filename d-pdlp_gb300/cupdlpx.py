@@ -175,6 +175,10 @@ class SolveInfo(C.Structure):
         ("device_seconds", C.c_double),
         ("refinement_rounds", C.c_int),
         ("precision", C.c_int),
+        ("primal_step_ms", C.c_double),
+        ("dual_step_ms", C.c_double),
+        ("timed_chunks", C.c_int),
+        ("fp64_finish", C.c_int),
     ]
 
 

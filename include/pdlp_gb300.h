@@ -31,6 +31,14 @@ typedef struct {
                                  first copy/kernel to the result on the host */
   int refinement_rounds;      /* FP32 rounds of a mixed-precision solve */
   int precision;              /* PDLP_PRECISION_* the solve ran in */
+  double primal_step_ms;      /* average device time of an ordinary primal-step
+                                 launch (A^T SpMV + update) inside the loop,
+                                 from CUDA events in one iteration per
+                                 100-iteration chunk */
+  double dual_step_ms;        /* the same for the dual step (A SpMV + update) */
+  int timed_chunks;           /* chunks those averages cover (0: none) */
+  int fp64_finish;            /* 1 when a mixed-precision solve ended with FP64
+                                 PDHG warm-started from its best FP64 point */
 } pdlp_solve_info_t;
 
 /* Arithmetic of the PDHG iteration.
@@ -39,7 +47,9 @@ typedef struct {
  *   accumulation); KKT / gap / restart / primal-weight reductions, objective
  *   values and the refinement residuals in FP64.  Rounds of iterative
  *   refinement re-centre the LP at the FP64 point until the FP64 KKT of the
- *   original problem meets the requested tolerances.
+ *   original problem meets the requested tolerances; when a round cannot
+ *   improve the point (an FP32 precision floor), FP64 PDHG finishes from the
+ *   best FP64 point.
  * The drop-in solve_lp_problem() uses FP64 unless the environment variable
  * PDLP_PRECISION is "fp32" (FP32_REFINE) or "fp32m" (FP32_MATRIX). */
 #define PDLP_PRECISION_FP64 0

@@ -26,6 +26,8 @@ STRUCTS = {"LpProblem": "lp_problem_t", "RestartParameters": "restart_parameters
            "TerminationCriteria": "termination_criteria_t", "GridSize": "grid_size_t",
            "PdhgParameters": "pdhg_parameters_t", "Result": "cupdlpx_result_t",
            "MatrixDesc": "matrix_desc_t"}
+# this library's own structures (include/pdlp_gb300.h)
+EXT_STRUCTS = {"SolveInfo": "pdlp_solve_info_t", "Options": "pdlp_options_t"}
 
 
 def declared_functions():
@@ -55,10 +57,10 @@ def test_library_exports_every_declared_function(lib, name):
     assert hasattr(lib, name), f"{name} declared in include/ but not exported"
 
 
-def _layout_program(tmp_path):
-    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "cupdlpx_types.h"',
+def _layout_program(tmp_path, structs, header):
+    lines = ["#include <stddef.h>", "#include <stdio.h>", f'#include "{header}"',
              "int main(void) {"]
-    for py, ct in STRUCTS.items():
+    for py, ct in structs.items():
         lines.append(f'  printf("{py} . %zu %zu\\n", sizeof({ct}), _Alignof({ct}));')
         for f, _t in getattr(cp, py)._fields_:
             lines.append(f'  printf("{py} {f} %zu %zu\\n", offsetof({ct}, {f}), '
@@ -69,8 +71,8 @@ def _layout_program(tmp_path):
     return src
 
 
-def _c_layout(tmp_path, incs, tag):
-    src = _layout_program(tmp_path)
+def _c_layout(tmp_path, incs, tag, structs=STRUCTS, header="cupdlpx_types.h"):
+    src = _layout_program(tmp_path, structs, header)
     exe = tmp_path / f"layout_{tag}"
     r = subprocess.run(["gcc", "-std=gnu11", *[f"-I{i}" for i in incs], str(src), "-o", str(exe)],
                        capture_output=True, text=True)
@@ -79,9 +81,9 @@ def _c_layout(tmp_path, incs, tag):
     return {(a, b): (int(c), int(d)) for a, b, c, d in (l.split() for l in out.splitlines())}
 
 
-def _ctypes_layout():
+def _ctypes_layout(structs=STRUCTS):
     lay = {}
-    for py in STRUCTS:
+    for py in structs:
         S = getattr(cp, py)
         lay[(py, ".")] = (C.sizeof(S), C.alignment(S))
         for f, t in S._fields_:
@@ -91,6 +93,8 @@ def _ctypes_layout():
 
 def test_ctypes_mirror_matches_c_header_layout(tmp_path):
     assert _c_layout(tmp_path, [INCLUDE], "ours") == _ctypes_layout()
+    assert _c_layout(tmp_path, [INCLUDE], "ext", EXT_STRUCTS, "pdlp_gb300.h") == \
+        _ctypes_layout(EXT_STRUCTS)
 
 
 def test_header_layout_matches_reference_header(tmp_path):

@@ -171,3 +171,26 @@ def test_repeat_solve_is_bitwise_reproducible(oracle):
     b = cp.solve(prob, p).result
     assert a["total_count"] == b["total_count"]
     assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["y"], b["y"])
+
+
+def test_in_loop_kernel_timing_is_reported(lib):
+    """Events captured into the chunk graphs time one ordinary primal and dual
+    launch per 100-iteration chunk; the averages agree with isolated launches."""
+    prob = cp.Problem.generated("random", 2000, 5000, 20000, 0)
+    params = cp.default_parameters()
+    params.presolve = False
+    dp = cp.DeviceProblem(prob)
+    try:
+        out = dp.solve(params)
+        info = out.info
+        assert out.result["status"] == "OPTIMAL"
+        assert info["timed_chunks"] >= out.result["total_count"] // 100 - 3
+        ms = dp.time_kernels(params, reps=10)
+        for live, iso in ((info["primal_step_ms"], ms[0]), (info["dual_step_ms"], ms[1])):
+            assert 0 < live < 5 * iso + 0.05, (live, iso)
+        # the sampled events leave the solve unchanged
+        again = dp.solve(params).result
+        assert again["total_count"] == out.result["total_count"]
+        assert np.array_equal(again["x"], out.result["x"])
+    finally:
+        dp.free()
