@@ -51,6 +51,26 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "powerlaw_m1M_n2M_nnz20M_seed1"
 
+# Many independent LPs: each generated as the random LP above, with m
+# log-uniform in [1,000, 100,000], n = 2.5 m and 10 non-zeros per column.
+BATCH_WORKLOADS = {
+    "batch_random_512_seed100": {
+        "lps": 512, "seed0": 100,
+        "desc": "512 random LPs (seeds 100..611), m log-uniform in [1e3, 1e5], n = 2.5 m, "
+                "10 nnz per column, FP64, eps 1e-4",
+    },
+}
+# Open-loop serving: Poisson arrivals; each request is drawn from a seeded
+# pool of LPs with the batch distribution, 10% of them large (m = 200,000,
+# n = 500,000, nnz = 5M).
+SERVE_WORKLOADS = {
+    "serve_poisson_seed7": {
+        "seed": 7, "rate": 200.0, "duration": 60.0, "pool_small": 96, "pool_large": 4,
+        "desc": "Poisson arrivals (seed 7); requests from the batch distribution with 10% "
+                "large LPs (m=200,000 n=500,000 nnz=5M), FP64, eps 1e-4",
+    },
+}
+
 # Iteration counts of this algorithm on each seeded workload (FP64, eps 1e-4),
 # as measured by the GPU arm; the oracle runs the same schedule (its
 # evaluation trace matches the GPU's in the parity tests), so the reference
@@ -371,6 +391,159 @@ def run_kernels_only(args, cp):
                                         "eval_A": ms[2], "eval_AT": ms[3]}}))
 
 
+def batch_shapes(count, seed0):
+    """(m, n, nnz, seed) of the batch workload's LPs."""
+    import numpy as np
+    rng = np.random.default_rng(seed0)
+    out = []
+    for i in range(count):
+        m = int(np.exp(rng.uniform(np.log(1e3), np.log(1e5))))
+        n = int(2.5 * m)
+        out.append((m, n, 10 * n, seed0 + i))
+    return out
+
+
+def generate_parallel(cp, shapes, threads=None):
+    """Generate random LPs on host threads (the generator releases the GIL)."""
+    import concurrent.futures as cf
+    threads = threads or min(32, os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(lambda sh: cp.Problem.generated("random", *sh), shapes))
+
+
+def run_batch(args, cp):
+    """Batched LPs/s of pdlp_batch_solve against the same LPs solved one after
+    another through solve_lp_problem."""
+    w = BATCH_WORKLOADS[args.workload]
+    count = args.batch_lps or w["lps"]
+    shapes = batch_shapes(count, w["seed0"])
+    lps = generate_parallel(cp, shapes)
+    nnz_total = sum(sh[2] for sh in shapes)
+    params = params_for(cp, args.eps)
+    for _ in range(args.warmup):
+        cp.batch_solve(lps, params, workers=args.workers)
+    vals, iters = [], 0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            res, info = cp.batch_solve(lps, params, workers=args.workers)
+            vals.append(info["lps_per_second"])
+            iters = info["iterations"]
+            failed = info["failed"]
+    clocks = clk.summary()
+    # the same LPs one after another (our FP64 path, one stream)
+    t0 = time.perf_counter()
+    seq = [cp.solve(lp, params).result for lp in lps]
+    t_seq = time.perf_counter() - t0
+    same = all(a is not None and a["total_count"] == b["total_count"] for a, b in zip(res, seq))
+    value = statistics.mean(vals)
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the FP64 oracle on every host core, LPs in batch order for ~15 s
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        O = oracle_lib.load()
+        t0, k = time.perf_counter(), 0
+        while k < count and time.perf_counter() - t0 < 15.0:
+            oracle_lib.oracle_solve(O, lps[k], params)
+            k += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": round(k / el, 3), "unit": "LPs/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": f"the first {k} LPs of the batch solved by the FP64 "
+                                         f"oracle in {el:.1f} s"}
+    line = {
+        "metric": "batched LPs/s", "value": round(value, 2), "unit": "LPs/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(count / value * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": args.workload, "description": w["desc"], "lps": count,
+                   "nnz_total": nnz_total, "workers": args.workers, "eps": args.eps,
+                   "l2": "inputs larger than L2; no flush needed"},
+        "e2e": {"value": round(value, 2), "unit": "LPs/s",
+                "h2d_bytes_per_step": int(sum(24 * sh[2] + 32 * sh[1] + 20 * sh[0]
+                                              for sh in shapes)),
+                "d2h_bytes_per_step": int(sum(8 * (2 * sh[1] + sh[0]) for sh in shapes)),
+                "api": "pdlp_batch_solve from host arrays (upload, solve, copy-back per LP)"},
+        "sequential": {"lps_per_second": round(count / t_seq, 2), "seconds": round(t_seq, 2),
+                       "api": "solve_lp_problem, one LP after another"},
+        "batch": {"iterations": iters, "failed": failed, "max_concurrent": info["max_concurrent"],
+                  "results_match_sequential": same},
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+def run_serve(args, cp):
+    """Open-loop serving: requests arrive by a Poisson process; latency runs
+    from the scheduled arrival to the result on the host."""
+    import numpy as np
+    w = SERVE_WORKLOADS[args.workload]
+    rate = args.rate or w["rate"]
+    duration = args.duration or w["duration"]
+    rng = np.random.default_rng(w["seed"])
+    shapes = batch_shapes(w["pool_small"], 7000)
+    shapes += [(200000, 500000, 5000000, 8000 + i) for i in range(w["pool_large"])]
+    pool = generate_parallel(cp, shapes)
+    arrivals, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        large = rng.random() < 0.1
+        idx = (w["pool_small"] + int(rng.integers(w["pool_large"]))) if large else \
+            int(rng.integers(w["pool_small"]))
+        arrivals.append((t, idx))
+    params = params_for(cp, args.eps)
+    import threading
+    lat, done_t = [None] * len(arrivals), [None] * len(arrivals)
+    with cp.Server(params, workers=args.workers) as srv:
+        ids = [None] * len(arrivals)
+        t0 = time.perf_counter()
+
+        def collect():
+            for k in range(len(arrivals)):
+                while ids[k] is None:
+                    time.sleep(0.0005)
+                res, info = srv.wait(ids[k])
+                done_t[k] = time.perf_counter() - t0
+                lat[k] = done_t[k] - arrivals[k][0]
+
+        th = threading.Thread(target=collect)
+        with ClockSampler(0) as clk:
+            th.start()
+            for k, (ta, idx) in enumerate(arrivals):
+                d = ta - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                ids[k] = srv.submit(pool[idx])
+            th.join()
+        st = srv.stats()
+    clocks = clk.summary()
+    total = max(done_t)
+    lat_ms = np.array(lat) * 1e3
+    line = {
+        "metric": "served LPs/s; p50/p99 latency", "value": round(len(arrivals) / total, 2),
+        "unit": "LPs/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": round(total * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": args.workload, "description": w["desc"], "rate_per_s": rate,
+                   "duration_s": duration, "requests": len(arrivals), "workers": args.workers,
+                   "pool": f"{w['pool_small']} batch-distribution LPs + {w['pool_large']} large",
+                   "eps": args.eps},
+        "latency_ms": {"p50": round(float(np.percentile(lat_ms, 50)), 2),
+                       "p99": round(float(np.percentile(lat_ms, 99)), 2),
+                       "mean": round(float(lat_ms.mean()), 2),
+                       "max": round(float(lat_ms.max()), 2)},
+        "e2e": {"value": round(len(arrivals) / total, 2), "unit": "LPs/s",
+                "api": "pdlp_server_submit / pdlp_server_wait from host arrays"},
+        "server": {"completed": st["completed"], "failed": st["failed"],
+                   "max_in_flight": st["max_in_flight"], "iterations": st["iterations"]},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args, cp, rank):
     name = args.workload
     counts = REFERENCE_COUNTS.get(name, {})
@@ -409,7 +582,16 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) +
+                    sorted(SERVE_WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workers", type=int, default=8,
+                    help="batch / serving workload: worker threads (one CUDA stream each)")
+    ap.add_argument("--batch-lps", type=int, default=0,
+                    help="batch workload: number of LPs (0: the workload's 512)")
+    ap.add_argument("--rate", type=float, default=0.0,
+                    help="serving workload: arrivals per second (0: the workload's 200)")
+    ap.add_argument("--duration", type=float, default=0.0,
+                    help="serving workload: arrival window in seconds (0: the workload's 60)")
     ap.add_argument("--eps", type=float, default=1e-4)
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -433,6 +615,16 @@ def main():
     if args.kernels_only:
         if rank == 0:
             run_kernels_only(args, cp)
+        return
+    if args.workload in BATCH_WORKLOADS or args.workload in SERVE_WORKLOADS:
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "batched and served workloads have no CPU reference arm; "
+                                  "the sequential line is in the bench output"}))
+            return
+        if rank == 0:
+            (run_batch if args.workload in BATCH_WORKLOADS else run_serve)(args, cp)
         return
     if args.impl == "reference":
         if rank == 0:

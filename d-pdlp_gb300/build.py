@@ -21,8 +21,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcupdlpx_gb300.so")
 
 SOURCES = ["solver.cu", "solver_f32.cu", "solver_mix.cu", "refine.cu", "precond.cu", "hooks.cu",
-           "noalloc.cu",
-           "api.cpp", "lpgen.cpp"]
+           "noalloc.cu", "memory.cu",
+           "api.cpp", "serve.cpp", "lpgen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,9 +38,9 @@ def _flags(src: str) -> list[str]:
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC] + ARCH
     if src == "lpgen.cpp":
         f += ["-Xcompiler", "-ffp-contract=off"]  # bit-identical on x86 and Arm
-    if src.endswith(".cu") or src == "api.cpp":
+    if src.endswith(".cu") or src in ("api.cpp", "serve.cpp"):
         f += ["--expt-relaxed-constexpr"]
-    if src == "api.cpp":
+    if src in ("api.cpp", "serve.cpp"):
         f = ["-x", "cu"] + f  # includes the device-side solver header
     return f
 

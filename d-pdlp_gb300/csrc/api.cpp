@@ -19,6 +19,7 @@
 
 #include "cupdlpx.h"
 #include "pdlp_gb300.h"
+#include "runtime.h"
 #include "solver.cuh"
 
 struct pdlp_device_problem {
@@ -382,6 +383,25 @@ cupdlpx_result_t *solve_impl(const lp_problem_t *prob, const pdhg_parameters_t *
 
 }  // namespace
 
+namespace pdlp {
+
+cupdlpx_result_t *solve_uploaded(const DevProblem &P, const pdhg_parameters_t &p,
+                                 const pdlp_options_t &o, cudaStream_t st,
+                                 pdlp_solve_info_t *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  return o.precision != PDLP_PRECISION_FP64
+             ? run_refined(P, p, o, st, info, t0)
+             : run_solve(P, p, st, nullptr, 0, nullptr, info, t0);
+}
+
+bool resolve_parameters(const pdhg_parameters_t *params, pdhg_parameters_t &p) {
+  return prepare_params(params, p);
+}
+
+void record_error(const std::string &msg) { set_error(msg); }
+
+}  // namespace pdlp
+
 extern "C" {
 
 lp_problem_t *create_lp_problem(const double *objective_c, const matrix_desc_t *A_desc,
@@ -572,7 +592,10 @@ int pdlp_gpu_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params, 
     const pdlp::Dev<double> &d = s.dev();
     const int n = d.n, m = d.m, nnz = s.A().nnz;
     auto get = [&](double *dst, const double *src, int cnt) {
-      if (cnt > 0) PDLP_CUDA(cudaMemcpy(dst, src, (size_t)cnt * 8, cudaMemcpyDeviceToHost));
+      if (cnt > 0) {
+        PDLP_CUDA(cudaMemcpyAsync(dst, src, (size_t)cnt * 8, cudaMemcpyDeviceToHost, sg.s));
+        PDLP_CUDA(cudaStreamSynchronize(sg.s));
+      }
     };
     get(vals, s.A64().val, nnz);
     get(c, d.c, n);

@@ -97,6 +97,17 @@ struct HostFlag {
   volatile int pm_done;
 };
 
+// Device memory of the solve path: a stream-ordered pool owned by the library
+// (no device-wide synchronisation, unlike cudaMalloc / cudaFree); a block
+// freed on a stream is reused by later allocations (memory.cu).
+void *dev_alloc(size_t bytes, cudaStream_t st);
+void dev_free(void *p, cudaStream_t st);
+// Mapped pinned termination flags from a slab allocated once.
+HostFlag *hostflag_acquire();
+void hostflag_release(HostFlag *f);
+// Return the pool's cached blocks to the device.
+void release_pooled_memory();
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

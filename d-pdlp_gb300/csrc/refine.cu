@@ -135,12 +135,12 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   for (int i = 0; i < 7; ++i) need(vm * 8);  // ybar w lc2 uc2 lcf ucf yold
   need((size_t)P.A.plan.nlong * 4); need((size_t)P.A.plan.nblk * 8);
   need((size_t)P.AT.plan.nlong * 4); need((size_t)P.AT.plan.nblk * 8);
-  char *mem = nullptr;
-  PDLP_CUDA(cudaMalloc(&mem, bytes));
+  char *mem = (char *)dev_alloc(bytes, st);
   struct Free {
     char *p;
-    ~Free() { cudaFree(p); }
-  } guard{mem};
+    cudaStream_t s;
+    ~Free() { dev_free(p, s); }
+  } guard{mem, st};
   size_t off = 0;
   auto take = [&](size_t b) {
     char *p = mem + off;

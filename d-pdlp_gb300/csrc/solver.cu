@@ -106,7 +106,8 @@ static int pick_tile(long nnz) {
 }
 
 DevProblem::~DevProblem() {
-  if (arena) cudaFree(arena);
+  // no work of any solve is in flight on the problem when it is freed
+  if (arena) dev_free(arena, cudaStreamPerThread);
 }
 
 DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
@@ -176,7 +177,7 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   for (int i = 0; i < 2; ++i) z.add<double>(vm);
   if (prob->primal_start) z.add<double>(vn);
   if (prob->dual_start) z.add<double>(vm);
-  PDLP_CUDA(cudaMalloc(&P->arena, z.bytes));
+  P->arena = dev_alloc(z.bytes, st);
   P->bytes = z.bytes;
   Arena ar{(char *)P->arena, 0};
   auto mat = [&](DevCsr &M, int rows, int cols, std::vector<int4> &blk, std::vector<int2> &lr) {

@@ -226,6 +226,10 @@ class Solve {
 
  private:
   void alloc();
+  void read_ctl(Ctl &c) const {
+    PDLP_CUDA(cudaMemcpyAsync(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaStreamSynchronize(st_));
+  }
   void enqueue_iteration(int t, int off, bool timed = false);
   void enqueue_eval(int off, bool infeas, bool restart_check, int mode);
   cudaGraphExec_t chunk_graph(int t0, int t1);

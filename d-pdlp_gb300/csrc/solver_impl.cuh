@@ -416,14 +416,14 @@ Solve<T, M>::Solve(const pdhg_parameters_t &params, cudaStream_t stream, const D
 
 template <class T, class M>
 Solve<T, M>::~Solve() {
-  if (snap_mem_) cudaFree(snap_mem_);
+  if (snap_mem_) dev_free(snap_mem_, st_);
   for (auto &slot : tev_)
     for (auto ev : slot)
       if (ev) cudaEventDestroy(ev);
   for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
   for (auto g : raw_graphs_) cudaGraphDestroy(g);
-  if (arena_) cudaFree(arena_);
-  if (hflag_) cudaFreeHost(hflag_);
+  if (arena_) dev_free(arena_, st_);
+  hostflag_release(hflag_);
 }
 
 template <class T, class M>
@@ -461,7 +461,7 @@ void Solve<T, M>::alloc() {
   z.add<double>(pa * 2); z.add<double>((size_t)ew);           // power partials
   z.add<double>((size_t)kMiscPart);
   z.add<Ctl>(1); z.add<double>((size_t)trace_cap_ * 10 + 1);
-  PDLP_CUDA(cudaMalloc(&arena_, z.bytes));
+  arena_ = dev_alloc(z.bytes, st_);
   Arena ar{(char *)arena_, 0};
 
   auto mat64 = [&](DevCsr &W, const DevCsr &S) {
@@ -532,7 +532,7 @@ void Solve<T, M>::alloc() {
   d.trace = trace_cap_ > 0 ? ar.take<double>((size_t)trace_cap_ * 10) : nullptr;
   d.trace_cap = trace_cap_;
 
-  PDLP_CUDA(cudaHostAlloc((void **)&hflag_, sizeof(HostFlag), cudaHostAllocMapped));
+  hflag_ = hostflag_acquire();
   hflag_->done = 0;
   hflag_->pm_done = 0;
   HostFlag *dflag = nullptr;
@@ -747,8 +747,7 @@ void Solve<T, M>::enable_snapshot() {
   if (snapshot_) return;
   Dev<T> &d = d_;
   size_t bytes = ((size_t)d.n * 2 + d.m) * sizeof(T) + 1024;
-  void *mem = nullptr;
-  PDLP_CUDA(cudaMalloc(&mem, bytes));
+  void *mem = dev_alloc(bytes, st_);
   snap_mem_ = mem;
   d.bx = (T *)mem;
   d.bl = d.bx + d.n;
@@ -759,7 +758,7 @@ void Solve<T, M>::enable_snapshot() {
 template <class T, class M>
 double Solve<T, M>::primal_weight() const {
   Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  read_ctl(c);
   return c.primal_weight;
 }
 
@@ -1005,24 +1004,25 @@ void Solve<T, M>::time_kernels(int reps, double *ms) {
 template <class T, class M>
 int Solve<T, M>::reason() const {
   Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  read_ctl(c);
   return c.reason;
 }
 
 template <class T, class M>
 int Solve<T, M>::total_count() const {
   Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  read_ctl(c);
   return c.final_t;
 }
 
 template <class T, class M>
 std::vector<double> Solve<T, M>::trace() const {
   Ctl c;
-  PDLP_CUDA(cudaMemcpy(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  read_ctl(c);
   std::vector<double> tr((size_t)c.trace_len * 10);
   if (c.trace_len)
-    PDLP_CUDA(cudaMemcpy(tr.data(), d_.trace, tr.size() * 8, cudaMemcpyDeviceToHost));
+    PDLP_CUDA(cudaMemcpyAsync(tr.data(), d_.trace, tr.size() * 8, cudaMemcpyDeviceToHost, st_));
+    PDLP_CUDA(cudaStreamSynchronize(st_));
   return tr;
 }
 

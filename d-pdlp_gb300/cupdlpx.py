@@ -185,6 +185,25 @@ class SolveInfo(C.Structure):
 PRECISION_FP64, PRECISION_FP32_REFINE, PRECISION_FP32_MATRIX = 0, 1, 2
 
 
+class RequestInfo(C.Structure):
+    _fields_ = [("queued_seconds", C.c_double), ("solve_seconds", C.c_double),
+                ("latency_seconds", C.c_double), ("worker", C.c_int),
+                ("device_bytes", C.c_longlong)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("queued", C.c_longlong), ("in_flight", C.c_int), ("max_in_flight", C.c_int),
+                ("iterations", C.c_longlong), ("device_bytes_in_use", C.c_longlong),
+                ("busy_seconds", C.c_double)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("lps", C.c_int), ("failed", C.c_int), ("wall_seconds", C.c_double),
+                ("lps_per_second", C.c_double), ("iterations", C.c_longlong),
+                ("max_concurrent", C.c_int)]
+
+
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_refinements", C.c_int), ("inner_eps", C.c_double)]
 
@@ -247,6 +266,25 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_device_problem_time_kernels_prec.restype = C.c_int
     lib.pdlp_device_problem_time_kernels_prec.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                                           C.c_int, C.c_int, _dp]
+    lib.pdlp_estimate_device_bytes.restype = C.c_longlong
+    lib.pdlp_estimate_device_bytes.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_int]
+    lib.pdlp_server_create.restype = C.c_void_p
+    lib.pdlp_server_create.argtypes = [C.POINTER(PdhgParameters), C.POINTER(Options), C.c_int,
+                                       C.c_longlong]
+    lib.pdlp_server_submit.restype = C.c_longlong
+    lib.pdlp_server_submit.argtypes = [C.c_void_p, P]
+    lib.pdlp_server_wait.restype = R
+    lib.pdlp_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(RequestInfo)]
+    lib.pdlp_server_stats.restype = C.c_int
+    lib.pdlp_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.pdlp_server_destroy.restype = None
+    lib.pdlp_server_destroy.argtypes = [C.c_void_p]
+    lib.pdlp_batch_solve.restype = C.c_int
+    lib.pdlp_batch_solve.argtypes = [C.POINTER(P), C.c_int, C.POINTER(PdhgParameters),
+                                     C.POINTER(Options), C.c_int, C.c_longlong, C.POINTER(R),
+                                     C.POINTER(BatchInfo)]
+    lib.pdlp_release_pooled_memory.restype = None
+    lib.pdlp_release_pooled_memory.argtypes = []
     lib.pdlp_device_problem_time_kernels.restype = C.c_int
     lib.pdlp_device_problem_time_kernels.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                                      C.c_int, _dp]
@@ -477,3 +515,82 @@ class DeviceProblem:
             self.free()
         except Exception:
             pass
+
+
+class Server:
+    """Request loop over independent LPs (pdlp_server_t): `workers` threads,
+    each with its own CUDA stream, admitting LPs by device-memory budget."""
+
+    def __init__(self, params: PdhgParameters | None = None, precision: int = PRECISION_FP64,
+                 workers: int = 8, mem_budget_bytes: int = 0, library: C.CDLL | None = None):
+        self._lib = library or lib()
+        o = make_options(precision)
+        pp = C.byref(params) if params is not None else None
+        self.handle = self._lib.pdlp_server_create(pp, C.byref(o), workers, mem_budget_bytes)
+        if not self.handle:
+            raise RuntimeError("server creation failed: " + self._lib.pdlp_last_error().decode())
+
+    def submit(self, problem: Problem) -> int:
+        rid = self._lib.pdlp_server_submit(self.handle, problem.ptr)
+        if rid < 0:
+            raise RuntimeError("submit failed")
+        return rid
+
+    def wait(self, rid: int) -> tuple[dict, dict]:
+        info = RequestInfo()
+        r = self._lib.pdlp_server_wait(self.handle, rid, C.byref(info))
+        if not r:
+            raise RuntimeError("request failed: " + self._lib.pdlp_last_error().decode())
+        try:
+            res = result_dict(r)
+        finally:
+            self._lib.cupdlpx_result_free(r)
+        return res, {f: getattr(info, f) for f, _ in RequestInfo._fields_}
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self._lib.pdlp_server_stats(self.handle, C.byref(st))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            self._lib.pdlp_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_solve(problems: list, params: PdhgParameters | None = None,
+                precision: int = PRECISION_FP64, workers: int = 8, mem_budget_bytes: int = 0,
+                library: C.CDLL | None = None) -> tuple[list, dict]:
+    """Solve independent LPs side by side (pdlp_batch_solve); returns the
+    result dicts in input order and the batch statistics."""
+    L = library or lib()
+    n = len(problems)
+    arr = (C.POINTER(LpProblem) * n)(*[p.ptr for p in problems])
+    res = (C.POINTER(Result) * n)()
+    info = BatchInfo()
+    o = make_options(precision)
+    pp = C.byref(params) if params is not None else None
+    rc = L.pdlp_batch_solve(arr, n, pp, C.byref(o), workers, mem_budget_bytes, res,
+                            C.byref(info))
+    out = []
+    for i in range(n):
+        if res[i]:
+            out.append(result_dict(res[i]))
+            L.cupdlpx_result_free(res[i])
+        else:
+            out.append(None)
+    if rc not in (0, -3):
+        raise RuntimeError("batch failed: " + L.pdlp_last_error().decode())
+    return out, {f: getattr(info, f) for f, _ in BatchInfo._fields_}

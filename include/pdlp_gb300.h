@@ -119,6 +119,78 @@ int pdlp_device_problem_time_kernels_prec(pdlp_device_problem_t *dp,
                                           const pdhg_parameters_t *params,
                                           int precision, int reps, double *ms);
 
+/* ---- batched and served solves of independent LPs ----------------------
+ * No counterpart in the reference, which solves one LP per call
+ * (src/cupdlpx.c:174-198); each request runs that solve.
+ *
+ * A server runs `workers` host threads, each with its own CUDA stream, over
+ * one FIFO queue of submitted LPs (deep copies).  The head request is
+ * admitted when its estimated device footprint
+ * (pdlp_estimate_device_bytes) fits in what is left of the memory budget
+ * (mem_budget_bytes <= 0: 80% of the device memory free at creation); a
+ * request larger than the whole budget is admitted alone.  LPs in flight
+ * overlap on the GPU.  Each LP's arithmetic depends on its own data only, so
+ * its result is bitwise the same solved alone or in any mix.  All solves use
+ * `params` (NULL: defaults) and `opts` (NULL: FP64). */
+typedef struct pdlp_server pdlp_server_t;
+
+typedef struct {
+  double queued_seconds;    /* submit -> admission */
+  double solve_seconds;     /* admission -> result (upload, solve, copy back) */
+  double latency_seconds;   /* submit -> result */
+  int worker;               /* worker thread that solved it */
+  long long device_bytes;   /* footprint the admission charged */
+} pdlp_request_info_t;
+
+typedef struct {
+  long long completed;      /* requests finished (solved or failed) */
+  long long failed;         /* requests whose solve returned no result */
+  long long queued;         /* requests waiting for admission */
+  int in_flight;            /* requests being solved now */
+  int max_in_flight;        /* most requests in flight at once */
+  long long iterations;     /* PDHG iterations summed over finished requests */
+  long long device_bytes_in_use; /* footprint of the requests in flight */
+  double busy_seconds;      /* first admission to last finish */
+} pdlp_server_stats_t;
+
+/* Estimated device bytes of one solve (problem plus solve workspace). */
+long long pdlp_estimate_device_bytes(int m, int n, long long nnz, int precision);
+
+pdlp_server_t *pdlp_server_create(const pdhg_parameters_t *params,
+                                  const pdlp_options_t *opts, int workers,
+                                  long long mem_budget_bytes);
+/* Queue a copy of prob; returns the request id (>= 0) or -1. */
+long long pdlp_server_submit(pdlp_server_t *s, const lp_problem_t *prob);
+/* Block until request `id` is solved; the result (NULL on failure, see
+ * pdlp_last_error) belongs to the caller; info may be NULL.  Each id can be
+ * collected once. */
+cupdlpx_result_t *pdlp_server_wait(pdlp_server_t *s, long long id,
+                                   pdlp_request_info_t *info);
+int pdlp_server_stats(pdlp_server_t *s, pdlp_server_stats_t *stats);
+/* Finish every queued request, stop the workers and free what was not
+ * collected. */
+void pdlp_server_destroy(pdlp_server_t *s);
+
+typedef struct {
+  int lps;                  /* LPs submitted */
+  int failed;               /* LPs without a result */
+  double wall_seconds;      /* first submission to last result */
+  double lps_per_second;    /* solved LPs / wall_seconds */
+  long long iterations;     /* PDHG iterations summed over the LPs */
+  int max_concurrent;       /* most LPs in flight at once */
+} pdlp_batch_info_t;
+
+/* Solve `count` LPs through a server of `workers` workers; results[i] is the
+ * result of probs[i] (caller frees each).  Returns 0, or -3 when some LP
+ * failed (its result NULL), -1/-2 on bad arguments / no server. */
+int pdlp_batch_solve(const lp_problem_t *const *probs, int count,
+                     const pdhg_parameters_t *params, const pdlp_options_t *opts,
+                     int workers, long long mem_budget_bytes,
+                     cupdlpx_result_t **results, pdlp_batch_info_t *info);
+
+/* Return the device memory cached by the library's pool. */
+void pdlp_release_pooled_memory(void);
+
 /* Message of the last failure in this thread ("" if none). */
 const char *pdlp_last_error(void);
 
