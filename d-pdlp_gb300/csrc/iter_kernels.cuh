@@ -19,10 +19,12 @@ namespace pdlp {
   __device__ void bind(const double *) {}
 
 // Halpern weight w = (k+1)/(k+2), k = inner iteration count
-// (reference pdlp_core_op.cu:559-567), formed once per block.
-__device__ __forceinline__ void halpern_weight(const Ctl *c, int off, double *sc) {
+// (reference pdlp_core_op.cu:559-567), once per block: from the solve's table
+// (the same quotients, computed once) or, past its end, by division.
+__device__ __forceinline__ void halpern_weight(const Ctl *c, const double *hw, int hw_len,
+                                               int off, double *sc) {
   int k = c->t_base + off - c->restart_t;
-  double w = (double)(k + 1) / (double)(k + 2);
+  double w = (k >= 0 && k < hw_len) ? hw[k] : (double)(k + 1) / (double)(k + 2);
   sc[0] = w;
   sc[1] = 1.0 - w;
 }
@@ -48,17 +50,32 @@ struct PrimalEpi {
     tau = (T)c->tau;
     return true;
   }
-  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
+  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, d.hw, d.hw_len, off, sc); }
   __device__ void bind(const double *sc) {
     w = (T)sc[0];
     omw = (T)sc[1];
   }
   __device__ M gather(int i) const { return (M)ycur[i]; }
+  struct Pre {
+    T xc, c, lv, uv, x0;
+  };
+  __device__ void preload(int j, Pre &p) const {
+    p.xc = xcur[j];
+    p.c = d.c[j];
+    p.lv = d.lv[j];
+    p.uv = d.uv[j];
+    p.x0 = d.x0[j];
+  }
   __device__ void row(int j, M sm, double *acc) const {
+    Pre p;
+    preload(j, p);
+    row_pre(j, sm, p, acc);
+  }
+  __device__ void row_pre(int j, M sm, const Pre &p, double *acc) const {
     T s = (T)sm;
-    T xc = xcur[j];
-    T t = xc - tau * (d.c[j] - s);
-    T xh = clamp_to(t, d.lv[j], d.uv[j]);
+    T xc = p.xc;
+    T t = xc - tau * (p.c - s);
+    T xh = clamp_to(t, p.lv, p.uv);
     if (MAJOR) {
       d.xhat[j] = xh;
       d.lam[j] = (xh - t) / tau;
@@ -71,7 +88,7 @@ struct PrimalEpi {
       acc[0] += (double)dd * (double)dd;
     }
     T refl = RHO1 ? xr : (T)d.rho * xr + (T)d.one_minus_rho * xc;
-    xnext[j] = w * refl + omw * d.x0[j];
+    xnext[j] = w * refl + omw * p.x0;
   }
 };
 
@@ -95,19 +112,33 @@ struct DualEpi {
     inv_sigma = (T)c->inv_sigma;
     return true;
   }
-  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, off, sc); }
+  __device__ void prologue(double *sc) const { halpern_weight(d.ctl, d.hw, d.hw_len, off, sc); }
   __device__ void bind(const double *sc) {
     w = (T)sc[0];
     omw = (T)sc[1];
   }
   __device__ M gather(int j) const { return (M)d.xref[j]; }
+  struct Pre {
+    T yc, lc, uc, y0;
+  };
+  __device__ void preload(int i, Pre &p) const {
+    p.yc = ycur[i];
+    p.lc = d.lc[i];
+    p.uc = d.uc[i];
+    p.y0 = d.y0[i];
+  }
   __device__ void row(int i, M sm, double *acc) const {
+    Pre p;
+    preload(i, p);
+    row_pre(i, sm, p, acc);
+  }
+  __device__ void row_pre(int i, M sm, const Pre &p, double *acc) const {
     T s = (T)sm;
-    T yc = ycur[i];
+    T yc = p.yc;
     // the reference divides by sigma; one reciprocal per launch instead
     // (at most 1 ulp apart; an FP64 division costs ~10 FP64 issue slots)
     T t = yc * inv_sigma - s;
-    T tp = clamp_to(t, -d.uc[i], -d.lc[i]);
+    T tp = clamp_to(t, -p.uc, -p.lc);
     T yh = (t - tp) * sigma;
     if (MAJOR) d.yhat[i] = yh;
     T yr = T(2) * yh - yc;
@@ -117,7 +148,7 @@ struct DualEpi {
       acc[0] += (double)dd * (double)dd;
     }
     T refl = RHO1 ? yr : (T)d.rho * yr + (T)d.one_minus_rho * yc;
-    ynext[i] = w * refl + omw * d.y0[i];
+    ynext[i] = w * refl + omw * p.y0;
   }
 };
 

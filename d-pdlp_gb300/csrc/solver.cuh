@@ -76,6 +76,10 @@ struct Dev {
   double *p_i2, *lp_i2;        // ray over A^T (3)
   double *p_rs;                // restart distances (2 x ew_grid)
   double *p_misc;              // kMiscPart doubles for set-up reductions
+  // Halpern weights w_k = (k+1)/(k+2) for k < hw_len, filled once per solve
+  // so the iteration kernels load them instead of dividing per block
+  const double *hw;
+  int hw_len;
 };
 
 // The power method always runs in FP64 on the FP64 scaled matrix.
@@ -90,6 +94,7 @@ struct PowDev {
 };
 
 constexpr int kMiscPart = 4096;
+constexpr int kHalpernTable = 1 << 16;
 
 // Termination reason of an FP32 refinement round that stopped improving;
 // internal, never returned to callers.

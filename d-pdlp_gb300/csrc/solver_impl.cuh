@@ -34,6 +34,7 @@ namespace pdlp {
 
 // Non-template kernels, defined in solver.cu.
 __global__ void k_set_tbase(Ctl *ctl, int t);
+__global__ void k_halpern_table(double *hw, int len);
 __global__ void k_loop_start(Ctl *ctl);
 __global__ void k_set_steps(Ctl *c);
 __global__ void k_pm_norm(PowDev d, const double *v);
@@ -460,6 +461,7 @@ void Solve<T, M>::alloc() {
   z.add<double>((size_t)ew * 2);                               // rs
   z.add<double>(pa * 2); z.add<double>((size_t)ew);           // power partials
   z.add<double>((size_t)kMiscPart);
+  z.add<double>((size_t)kHalpernTable);
   z.add<Ctl>(1); z.add<double>((size_t)trace_cap_ * 10 + 1);
   arena_ = dev_alloc(z.bytes, st_);
   Arena ar{(char *)arena_, 0};
@@ -528,6 +530,14 @@ void Solve<T, M>::alloc() {
   split(pw_.p_pa, pw_.lp_pa, nbA, nlA, 2);
   pw_.p_pr = ar.take<double>((size_t)ew);
   d.p_misc = ar.take<double>((size_t)kMiscPart);
+  {
+    double *hw = ar.take<double>((size_t)kHalpernTable);
+    k_halpern_table<<<grid_for(kHalpernTable), kThreads, 0, st_>>>(hw, kHalpernTable);
+    PDLP_LAUNCH_CHECK();
+    launches_ += 1;
+    d.hw = hw;
+    d.hw_len = kHalpernTable;
+  }
   d.ctl = ar.take<Ctl>(1);
   d.trace = trace_cap_ > 0 ? ar.take<double>((size_t)trace_cap_ * 10) : nullptr;
   d.trace_cap = trace_cap_;

@@ -28,6 +28,7 @@
 // single-block finaliser to fold in a fixed order.
 #pragma once
 
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -126,8 +127,34 @@ __device__ __forceinline__ int swz(int i) {
   return i ^ ((i >> (sizeof(T) == 8 ? 4 : 5)) & 7);
 }
 
+// Epilogues may define `struct Pre`, `preload(r, Pre&)` and
+// `row_pre(r, sum, const Pre&, acc)`: the stream path then issues each row's
+// vector loads in phase 1, next to the matrix stream, instead of after it.
+template <class E, class = void>
+struct has_preload : std::false_type {};
+template <class E>
+struct has_preload<E, std::void_t<typename E::Pre>> : std::true_type {};
+template <class E, bool = has_preload<E>::value>
+struct pre_of {
+  struct type {};
+};
+template <class E>
+struct pre_of<E, true> {
+  using type = typename E::Pre;
+};
+
+// Resident blocks per SM the register allocation must allow.  The kernel is
+// latency-bound (dependent col -> gather -> FMA chains, per-row vector loads),
+// so residency pays: 6 blocks of 256 threads (40 registers) for tiles of up
+// to 1024 non-zeros.  2048-element tiles need their registers (the long-row
+// path keeps 8 loads per thread in flight) and run at 4 blocks.
+template <int TILE>
+constexpr int spmv_min_blocks() {
+  return TILE >= 2048 ? 1 : 6;
+}
+
 template <int TILE, class Epi>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
     spmv_fused(const int *__restrict__ ptr, const int *__restrict__ col,
                const typename Epi::val_t *__restrict__ val, SpmvPlan plan,
                double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
@@ -136,7 +163,8 @@ __global__ void __launch_bounds__(kThreads)
   constexpr int NF = Epi::NF;
   constexpr int IPT = TILE / kThreads;
   constexpr int SEG = 8;  // elements per lane in the stream phase
-  __shared__ T sv[TILE];  // values; reused for stream-phase segment partials
+  __shared__ __align__(16) T sv[TILE];  // values; stream-phase segment partials;
+                                         // chunk partials of a long row (as doubles)
   __shared__ T sx[TILE];  // gathered x
   __shared__ int soff[kMaxRowsPerTile + 1];
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
@@ -152,6 +180,76 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
 
+  if (b.y < 0) {
+    // Chunk of a long row: each thread folds its IPT elements straight from
+    // global memory (coalesced loads, no shared staging); the 256 partials are
+    // summed in FP64 through shared memory -- warp 0 adds 8 per lane, then
+    // shuffles -- 13 FP64 warp instructions instead of a shuffle tree in every
+    // warp.  Rows of up to ~10^5 terms with cancellation keep every sum across
+    // threads, warps and chunks in FP64.
+    A s = A(0);
+    {
+      int cidx[IPT];
+      T v[IPT], xg[IPT];
+#pragma unroll
+      for (int u = 0; u < IPT; ++u) {
+        int i = threadIdx.x + u * kThreads;
+        if (i < len) {
+          cidx[u] = ld_stream(col + k0 + i);
+          v[u] = ld_stream(val + k0 + i);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < IPT; ++u)
+        if (threadIdx.x + u * kThreads < len) xg[u] = epi.gather(cidx[u]);
+#pragma unroll
+      for (int u = 0; u < IPT; ++u)
+        if (threadIdx.x + u * kThreads < len) s = fma((A)v[u], (A)xg[u], s);
+    }
+    double *tp = reinterpret_cast<double *>(sv);
+    tp[threadIdx.x] = (double)s;
+    __syncthreads();
+    epi.bind(sc);
+    const int lid = -b.y - 1;
+    if (threadIdx.x < 32) {
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) t += tp[threadIdx.x + 32 * w];
+      t = warp_sum(t);
+      if (threadIdx.x == 0) {
+        plan.lsum[blockIdx.x] = t;
+        __threadfence();
+        unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
+        s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
+      }
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      const int2 L = plan.lrow[lid];
+      double tot = 0.0;
+      for (int c = 0; c < L.y; ++c) tot += __ldcg(plan.lsum + L.x + c);
+      double lacc[NF > 0 ? NF : 1];
+#pragma unroll
+      for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
+      epi.row(b.x, (A)tot, lacc);
+      if constexpr (NF > 0) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
+      }
+      plan.lcnt[lid] = 0u;  // ready for the next launch
+    }
+    if constexpr (NF > 0) {
+      if (threadIdx.x == 0) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) part[f * plan.nblk + blockIdx.x] = 0.0;
+      }
+    }
+    return;
+  }
+
+  const bool stream = R > 1 && len <= 64 * R;
+  [[maybe_unused]] typename pre_of<Epi>::type pre;
   // Phase 1: coalesced stream of values / columns, gather of x, row offsets.
   {
     int cidx[IPT];
@@ -163,6 +261,9 @@ __global__ void __launch_bounds__(kThreads)
         sv[swz<T>(i)] = ld_stream(val + k0 + i);
       }
     }
+    if constexpr (has_preload<Epi>::value) {
+      if (stream && threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
+    }
     for (int j = threadIdx.x; j <= R; j += kThreads) soff[j] = ptr[b.x + j] - k0;
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
@@ -173,7 +274,7 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   epi.bind(sc);
 
-  if (b.y >= 0 && R > 1 && len <= 64 * R) {
+  if (stream) {
     // Stream phase: lane t folds elements [8t, 8t+8) with FMA, all lanes busy;
     // each finished segment's partial goes to sv[swz(start)], a slot the lane
     // has already consumed.
@@ -209,9 +310,14 @@ __global__ void __launch_bounds__(kThreads)
         sum = (A)sv[swz<T>(a)];
         for (int q = (a / SEG + 1) * SEG; q < e; q += SEG) sum += (A)sv[swz<T>(q)];
       }
-      epi.row(b.x + j, sum, acc);
+      if constexpr (has_preload<Epi>::value) {
+        if (j == (int)threadIdx.x) epi.row_pre(b.x + j, sum, pre, acc);
+        else epi.row(b.x + j, sum, acc);
+      } else {
+        epi.row(b.x + j, sum, acc);
+      }
     }
-  } else if (b.y >= 0) {
+  } else {
     const int r0 = b.x;
     if (R == 1) {
       // one long light row: lane chains in A, cross-lane sums in FP64
@@ -241,41 +347,6 @@ __global__ void __launch_bounds__(kThreads)
       double sd = s;  // cross-lane sums in FP64
       for (int o = G >> 1; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
       if (li == 0 && grp < R) epi.row(r0 + grp, (A)sd, acc);
-    }
-  } else {
-    // chunk of a long row: lane chains in A, every sum across lanes, warps
-    // and chunks in FP64 (rows of up to ~10^5 terms with cancellation)
-    A s = A(0);
-    for (int i = threadIdx.x; i < len; i += kThreads)
-      s = fma((A)sv[swz<T>(i)], (A)sx[swz<T>(i)], s);
-    double v = warp_sum((double)s);
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    const int lid = -b.y - 1;
-    if (threadIdx.x == 0) {
-      double tot = 0.0;
-      for (int w = 0; w < kThreads / 32; ++w) tot += red[w];
-      plan.lsum[blockIdx.x] = tot;
-      __threadfence();
-      unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
-      s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
-    }
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-      __threadfence();
-      const int2 L = plan.lrow[lid];
-      double tot = 0.0;
-      for (int c = 0; c < L.y; ++c) tot += __ldcg(plan.lsum + L.x + c);
-      double lacc[NF > 0 ? NF : 1];
-#pragma unroll
-      for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
-      epi.row(b.x, (A)tot, lacc);
-      if constexpr (NF > 0) {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
-      }
-      plan.lcnt[lid] = 0u;  // ready for the next launch
     }
   }
 
