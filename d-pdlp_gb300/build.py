@@ -22,7 +22,10 @@ LIB = os.path.join(HERE, "libcupdlpx_gb300.so")
 
 SOURCES = ["solver.cu", "solver_f32.cu", "solver_mix.cu", "refine.cu", "precond.cu", "hooks.cu",
            "noalloc.cu", "memory.cu",
-           "api.cpp", "serve.cpp", "lpgen.cpp"]
+           "api.cpp", "serve.cpp", "lpgen.cpp", "mps.cpp"]
+CLI = os.path.join(HERE, "cupdlpx")
+# gzip-compressed MPS input where the zlib header and library exist
+HAVE_ZLIB = os.path.exists("/usr/include/zlib.h")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -42,6 +45,8 @@ def _flags(src: str) -> list[str]:
         f += ["--expt-relaxed-constexpr"]
     if src in ("api.cpp", "serve.cpp"):
         f = ["-x", "cu"] + f  # includes the device-side solver header
+    if src == "mps.cpp" and HAVE_ZLIB:
+        f += ["-DPDLP_HAVE_ZLIB"]
     return f
 
 
@@ -69,10 +74,20 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, hdr), SOURCES))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-cudart", "static"]
+        cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-cudart", "static"] + \
+            (["-lz"] if HAVE_ZLIB else [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    src = os.path.join(CSRC, "cli.cpp")
+    if not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(LIB),
+                                                              os.path.getmtime(src), hdr):
+        # the command-line tool, linked against the library beside it
+        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+               src, "-o", CLI, "-L" + HERE, "-lcupdlpx_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(LIB)
     return LIB

@@ -266,6 +266,8 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_device_problem_time_kernels_prec.restype = C.c_int
     lib.pdlp_device_problem_time_kernels_prec.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                                           C.c_int, C.c_int, _dp]
+    lib.read_mps_file.restype = P
+    lib.read_mps_file.argtypes = [C.c_char_p]
     lib.pdlp_estimate_device_bytes.restype = C.c_longlong
     lib.pdlp_estimate_device_bytes.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_int]
     lib.pdlp_server_create.restype = C.c_void_p
@@ -391,6 +393,15 @@ class Problem:
         k0 = None if c0 is None else C.byref(C.c_double(c0))
         ptr = L.create_lp_problem(as_dp(arrs[0]), C.byref(d), as_dp(arrs[1]), as_dp(arrs[2]),
                                   as_dp(arrs[3]), as_dp(arrs[4]), k0)
+        return cls(ptr, L)
+
+    @classmethod
+    def from_mps(cls, path: str, library: C.CDLL | None = None) -> "Problem":
+        """read_mps_file (free-format MPS, .mps or .mps.gz)."""
+        L = library or lib()
+        ptr = L.read_mps_file(os.fsencode(path))
+        if not ptr:
+            raise ValueError(f"cannot read MPS file {path}")
         return cls(ptr, L)
 
     @classmethod

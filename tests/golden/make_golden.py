@@ -9,6 +9,7 @@ ones without the reference sources.
 
 Run (where the reference sources exist):
     make -C oracle ref && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py mps     # ref_mps.npz: read_mps_file on tests/golden/mps
 """
 from __future__ import annotations
 
@@ -207,5 +208,39 @@ def main():
     print(f"wrote {OUT} ({os.path.getsize(OUT)} bytes, {len(g)} arrays)")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and len(sys.argv) == 1:
     main()
+
+
+# ------------------------------------------------------------------ MPS
+MPS_DIR = os.path.join(HERE, "mps")
+MPS_OUT = os.path.join(HERE, "ref_mps.npz")
+
+
+def mps_main():
+    """The reference's read_mps_file on every fixture under tests/golden/mps."""
+    R = ol.load_ref()
+    if R is None:
+        sys.exit("oracle/_ref/libref_host.so is missing: run make -C oracle ref")
+    R.read_mps_file.restype = C.POINTER(cp.LpProblem)
+    R.read_mps_file.argtypes = [C.c_char_p]
+    g = {}
+    names = sorted(f for f in os.listdir(MPS_DIR) if ".mps" in f)
+    for name in names:
+        pp = R.read_mps_file(os.path.join(MPS_DIR, name).encode())
+        if not pp:
+            g[f"{name}__failed"] = np.array(1)
+            continue
+        a = cp.problem_arrays(pp)
+        for k in ("row_ptr", "col_ind", "vals", "c", "lc", "uc", "lv", "uv"):
+            g[f"{name}__{k}"] = a[k]
+        g[f"{name}__shape"] = np.array([a["m"], a["n"], a["nnz"]])
+        g[f"{name}__c0"] = np.array(a["c0"])
+        R.lp_problem_free(pp)
+    g["names"] = np.array(names)
+    np.savez_compressed(MPS_OUT, **g)
+    print(f"wrote {MPS_OUT} ({len(names)} files)")
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "mps":
+    mps_main()
