@@ -234,6 +234,38 @@ struct StreamGuard {
   }
 };
 
+// Feasibility polishing after an FP64 solve (reference src/pdlp_core_op.cu:
+// 862-930): when the solve's relative residuals are not both below
+// eps_feas_polish_relative, PDHG runs on the primal feasibility problem
+// (objective 0) and then on the dual one (finite bounds 0), each from the
+// solve's iterates with the initial primal weight, and the solve adopts each
+// side that reaches the tolerance.
+void feasibility_polish(const pdlp::DevProblem &P, const pdhg_parameters_t &p, cudaStream_t st,
+                        pdlp::Solve<double> &s, double &seconds, int &iterations) {
+  auto t0 = std::chrono::steady_clock::now();
+  const double eps = p.termination_criteria.eps_feas_polish_relative;
+  pdlp::Kkt k = s.last_kkt();
+  if (k.rel_p < eps && k.rel_d < eps) {
+    if (!quiet_summary())
+      printf("Skipping feasibility polishing as the solution is already sufficiently feasible.\n");
+    return;
+  }
+  const double w0 = p.bound_objective_rescaling
+                        ? 1.0
+                        : (s.dev().cnorm + 1.0) / (s.dev().bnorm + 1.0);
+  for (int mode = 1; mode <= 2; ++mode) {
+    pdlp::Solve<double> ps(p, st, P, 0);
+    ps.prepare();
+    ps.init_step(s.sigma_max(), w0);
+    ps.polish_init(s, mode);
+    ps.run();
+    if (ps.reason() == TERMINATION_REASON_FEAS_POLISH_SUCCESS) s.adopt_polish(ps, mode);
+    iterations += ps.total_count() - 1;
+  }
+  s.finish_polish();
+  seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &p,
                             cudaStream_t st, double *trace, int trace_cap, int *trace_len,
                             pdlp_solve_info_t *info,
@@ -250,7 +282,17 @@ cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &
   s.init_step();
   auto t2 = std::chrono::steady_clock::now();
   s.run();
+  double polish_sec = 0.0;
+  int polish_iters = 0;
+  const int why = s.reason();
+  if (p.feasibility_polishing && why != TERMINATION_REASON_PRIMAL_INFEASIBLE &&
+      why != TERMINATION_REASON_DUAL_INFEASIBLE)
+    feasibility_polish(P, p, st, s, polish_sec, polish_iters);
   cupdlpx_result_t *r = s.result();
+  if (r) {
+    r->feasibility_polishing_time = polish_sec;
+    r->feasibility_iteration = polish_iters;
+  }
   auto t3 = std::chrono::steady_clock::now();
   if (info) {
     PDLP_CUDA(cudaEventRecord(ev1, st));

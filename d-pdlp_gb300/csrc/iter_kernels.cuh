@@ -217,8 +217,8 @@ struct EvalATEpi {
       acc[2] += lam * d.Dc[j] / d.ob * d.sdd_inv * xo;
     } else {
       double xh = d.xhat[j];
-      acc[1] += c * xh;
-      acc[2] += lam * xh;
+      acc[1] += (double)d.c_obj[j] * xh;
+      acc[2] += lam * (double)d.x_obj[j];
     }
   }
 };

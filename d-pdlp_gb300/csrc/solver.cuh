@@ -76,6 +76,13 @@ struct Dev {
   double *p_i2, *lp_i2;        // ray over A^T (3)
   double *p_rs;                // restart distances (2 x ew_grid)
   double *p_misc;              // kMiscPart doubles for set-up reductions
+  // feasibility polishing (reference src/pdlp_core_op.cu:861-1360): 0 for a
+  // solve, 1 / 2 for the primal / dual feasibility problem, which evaluate
+  // and restart one side only; c_obj / x_obj are the objective and primal
+  // point the objective terms use (c and x_hat, or the solve's for polishing)
+  int polish;
+  double eps_polish;
+  const T *c_obj, *x_obj;
   // Halpern weights w_k = (k+1)/(k+2) for k < hw_len, filled once per solve
   // so the iteration kernels load them instead of dividing per block
   const double *hw;
@@ -208,6 +215,19 @@ class Solve {
   double live_dual_ms() const;
   int live_samples() const;
 
+  // Feasibility polishing (reference src/pdlp_core_op.cu:861-1360).  After
+  // prepare() and init_step(main's sigma, w0): turn this solve into the
+  // primal (mode 1: objective 0, dual iterates 0) or dual (mode 2: finite
+  // bounds 0, primal iterates 0) feasibility problem of `main`, starting
+  // from main's final iterates.
+  void polish_init(const Solve &main, int mode);
+  // Take a successful polish's point and residuals (mode 1 primal, 2 dual);
+  // finish_polish() then recomputes the gap from the objectives.
+  void adopt_polish(const Solve &ps, int mode);
+  void finish_polish();
+  // FP64 KKT scalars of the last evaluation (scaled problem, original units)
+  Kkt last_kkt() const;
+
   // diagnostics
   int power_iterations() const { return pm_iters_; }
   double sigma_max() const { return sigma_max_; }
@@ -231,6 +251,12 @@ class Solve {
 
  private:
   void alloc();
+  // schedule of iteration t (polishing never runs infeasibility detection)
+  IterFlags flags(int t) const {
+    IterFlags f = iteration_flags(t, d_.F);
+    if (d_.polish) f.infeas = false;
+    return f;
+  }
   void read_ctl(Ctl &c) const {
     PDLP_CUDA(cudaMemcpyAsync(&c, d_.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st_));
     PDLP_CUDA(cudaStreamSynchronize(st_));

@@ -96,20 +96,23 @@ __global__ void __launch_bounds__(kThreads) k_restart(Dev<T> d, T *xcur, T *ycur
   __shared__ double red[24];
   double a[2] = {0.0, 0.0};
   long stride = (long)gridDim.x * kThreads;
-  for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
-    T xh = d.xhat[j];
-    double dd = (double)xh - (double)d.x0[j];
-    a[0] += dd * dd;
-    d.x0[j] = xh;
-    xcur[j] = xh;
-  }
-  for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
-    T yh = d.yhat[i];
-    double dd = (double)yh - (double)d.y0[i];
-    a[1] += dd * dd;
-    d.y0[i] = yh;
-    ycur[i] = yh;
-  }
+  // polishing restarts one side (reference perform_primal / dual_restart)
+  if (d.polish != 2)
+    for (long j = blockIdx.x * (long)kThreads + threadIdx.x; j < d.n; j += stride) {
+      T xh = d.xhat[j];
+      double dd = (double)xh - (double)d.x0[j];
+      a[0] += dd * dd;
+      d.x0[j] = xh;
+      xcur[j] = xh;
+    }
+  if (d.polish != 1)
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < d.m; i += stride) {
+      T yh = d.yhat[i];
+      double dd = (double)yh - (double)d.y0[i];
+      a[1] += dd * dd;
+      d.y0[i] = yh;
+      ycur[i] = yh;
+    }
   block_reduce_fields<2, 0u>(a, red);
   if (threadIdx.x == 0) {
     d.p_rs[blockIdx.x] = a[0];
@@ -126,6 +129,11 @@ __global__ void __launch_bounds__(kThreads) k_restart_fin(Dev<T> d, int off) {
   double ps = block_fold<false>(d.p_rs, d.ew_grid, sm);
   double ds = block_fold<false>(d.p_rs + d.ew_grid, d.ew_grid, sm);
   if (threadIdx.x != 0) return;
+  if (d.polish) {  // polishing keeps the primal weight
+    c->restart_t = c->t_base + off;
+    c->last_trial_fixed_point_error = INFINITY;
+    return;
+  }
   double pd = sqrt(ps), dd = sqrt(ds);
   double ratio = c->rel_dual_res / c->rel_primal_res;
   if (pd > 1e-16 && dd > 1e-16 && pd < 1e12 && dd < 1e12 && ratio > 1e-8 && ratio < 1e8) {
@@ -164,9 +172,15 @@ __global__ void __launch_bounds__(kThreads) k_fpe_fin(Dev<T> d, int restart_only
   if (threadIdx.x != 0) return;
   double pn = sqrt(pn2), dn = sqrt(dn2);
   double w = c->primal_weight;
-  double movement = pn * pn * w + dn * dn / w;
-  double interaction = 2 * c->step_size * cross;
-  c->fixed_point_error = sqrt(movement + interaction);
+  if (d.polish == 1) {  // reference compute_primal_fixed_point_error
+    c->fixed_point_error = pn * pn * w;
+  } else if (d.polish == 2) {  // reference compute_dual_fixed_point_error
+    c->fixed_point_error = dn * dn / w;
+  } else {
+    double movement = pn * pn * w + dn * dn / w;
+    double interaction = 2 * c->step_size * cross;
+    c->fixed_point_error = sqrt(movement + interaction);
+  }
   if (c->do_restart) {
     c->initial_fixed_point_error = c->fixed_point_error;
     c->do_restart = 0;
@@ -231,32 +245,44 @@ __global__ void __launch_bounds__(kThreads)
   c->cum_time = (double)(global_ns() - c->t_start_ns) * 1e-9;
   int reason = TERMINATION_REASON_UNSPECIFIED;
   bool stalled = false;
-  if (d.stall_min > 0 && mode == kEvalCheck) {
-    // best-iterate snapshot and stall rule of the refinement rounds
-    double err = fmax(c->rel_primal_res, fmax(c->rel_dual_res, c->rel_gap));
-    c->snap_now = err < c->snap_err ? 1 : 0;
-    if (c->snap_now) c->snap_err = err;
-    if (err < 0.9 * c->best_err) {
-      c->best_err = err;
-      c->best_err_t = t;
-    } else if (t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
-      stalled = true;
+  if (d.polish) {
+    // reference check_feas_polishing_termination_criteria (utils.cu:1015-1039);
+    // the other side's residual and the gap are not measured
+    if (d.polish == 1) c->abs_dual_res = c->rel_dual_res = 0.0;
+    else c->abs_primal_res = c->rel_primal_res = 0.0;
+    c->gap = c->rel_gap = 0.0;
+    const double r = d.polish == 1 ? c->rel_primal_res : c->rel_dual_res;
+    if (r <= d.eps_polish) reason = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+    else if (mode == kEvalIterLimit) reason = TERMINATION_REASON_ITERATION_LIMIT;
+    else if (c->cum_time >= d.time_limit) reason = TERMINATION_REASON_TIME_LIMIT;
+  } else {
+    if (d.stall_min > 0 && mode == kEvalCheck) {
+      // best-iterate snapshot and stall rule of the refinement rounds
+      double err = fmax(c->rel_primal_res, fmax(c->rel_dual_res, c->rel_gap));
+      c->snap_now = err < c->snap_err ? 1 : 0;
+      if (c->snap_now) c->snap_err = err;
+      if (err < 0.9 * c->best_err) {
+        c->best_err = err;
+        c->best_err_t = t;
+      } else if (t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
+        stalled = true;
+      }
     }
-  }
-  if (mode == kEvalIterLimit) {
-    reason = TERMINATION_REASON_ITERATION_LIMIT;
-  } else if (c->rel_dual_res < d.eps_feas && c->rel_primal_res < d.eps_feas &&
-             c->rel_gap < d.eps_opt) {
-    reason = TERMINATION_REASON_OPTIMAL;
-  } else if (c->dual_ray_obj > 0.0 && c->max_dual_ray_inf / c->dual_ray_obj <= d.eps_inf) {
-    reason = TERMINATION_REASON_PRIMAL_INFEASIBLE;
-  } else if (c->primal_ray_obj < 0.0 &&
-             c->max_primal_ray_inf / (-c->primal_ray_obj) <= d.eps_inf) {
-    reason = TERMINATION_REASON_DUAL_INFEASIBLE;
-  } else if (c->cum_time >= d.time_limit) {
-    reason = TERMINATION_REASON_TIME_LIMIT;
-  } else if (stalled) {
-    reason = kReasonStalled;
+    if (mode == kEvalIterLimit) {
+      reason = TERMINATION_REASON_ITERATION_LIMIT;
+    } else if (c->rel_dual_res < d.eps_feas && c->rel_primal_res < d.eps_feas &&
+               c->rel_gap < d.eps_opt) {
+      reason = TERMINATION_REASON_OPTIMAL;
+    } else if (c->dual_ray_obj > 0.0 && c->max_dual_ray_inf / c->dual_ray_obj <= d.eps_inf) {
+      reason = TERMINATION_REASON_PRIMAL_INFEASIBLE;
+    } else if (c->primal_ray_obj < 0.0 &&
+               c->max_primal_ray_inf / (-c->primal_ray_obj) <= d.eps_inf) {
+      reason = TERMINATION_REASON_DUAL_INFEASIBLE;
+    } else if (c->cum_time >= d.time_limit) {
+      reason = TERMINATION_REASON_TIME_LIMIT;
+    } else if (stalled) {
+      reason = kReasonStalled;
+    }
   }
   if (d.trace && c->trace_len < d.trace_cap) {
     double *r = d.trace + (long)c->trace_len * 10;
@@ -278,7 +304,8 @@ __global__ void __launch_bounds__(kThreads)
            c->rel_primal_res, c->rel_dual_res, c->rel_gap);
   if (reason != TERMINATION_REASON_UNSPECIFIED) {
     c->reason = reason;
-    c->final_t = t;
+    // a polish loop completes the iteration in progress before it stops
+    c->final_t = d.polish ? t + 1 : t;
     c->done = 1;
     __threadfence_system();
     d.hflag->done = 1;
@@ -573,6 +600,10 @@ void Solve<T, M>::prepare() {
   d.oc0 = P_.orig_c0;
   d.sdp_inv = 1.0 / P_.delta_p;
   d.sdd_inv = 1.0 / P_.delta_d;
+  d.polish = 0;
+  d.eps_polish = p_.termination_criteria.eps_feas_polish_relative;
+  d.c_obj = d.c;
+  d.x_obj = d.xhat;
   d.rho = p_.reflection_coefficient;
   d.one_minus_rho = 1.0 - d.rho;
   d.rho_is_one = d.rho == 1.0;
@@ -775,7 +806,7 @@ double Solve<T, M>::primal_weight() const {
 template <class T, class M>
 void Solve<T, M>::enqueue_iteration(int t, int off, bool timed) {
   Dev<T> &d = d_;
-  IterFlags f = iteration_flags(t, d.F);
+  IterFlags f = flags(t);
   const int par = t & 1;
   T *xc = d.x[par], *xn = d.x[par ^ 1];
   T *yc = d.y[par], *yn = d.y[par ^ 1];
@@ -839,7 +870,7 @@ cudaGraphExec_t Solve<T, M>::chunk_graph(int t0, int t1) {
   key.reserve((size_t)(t1 - t0) * 2 + 2);
   key += (char)('0' + (t0 & 1));
   for (int t = t0; t < t1; ++t) {
-    IterFlags f = iteration_flags(t, d_.F);
+    IterFlags f = flags(t);
     key += (char)('A' + (f.eval) + 2 * f.infeas + 4 * f.restart_check + 8 * f.maybe_restart);
     key += (char)('A' + (f.major_kernel) + 2 * f.fpe + 4 * f.fpe_restart_only);
   }
@@ -887,7 +918,7 @@ cudaGraphExec_t Solve<T, M>::chunk_graph(int t0, int t1) {
 template <class T, class M>
 int Solve<T, M>::timed_iteration(int t0, int t1) const {
   for (int t = t0 + (t1 - t0) / 2; t < t1; ++t) {
-    IterFlags f = iteration_flags(t, d_.F);
+    IterFlags f = flags(t);
     if (!f.eval && !f.maybe_restart && !f.major_kernel && !f.fpe) return t;
   }
   return -1;
@@ -963,7 +994,7 @@ void Solve<T, M>::run() {
     PDLP_LAUNCH_CHECK();
     PDLP_CUDA(cudaGraphLaunch(g, st_));
     PDLP_CUDA(cudaEventRecord(ev[k & 1], st_));
-    for (int tt = t; tt < t1; ++tt) launches_ += iteration_launches(iteration_flags(tt, d.F));
+    for (int tt = t; tt < t1; ++tt) launches_ += iteration_launches(flags(tt));
     launches_ += 1;
     ++k;
     t = t1;
@@ -982,6 +1013,116 @@ void Solve<T, M>::run() {
   }
   loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   final_count_ = total_count();
+}
+
+// finite entries -> 0 (the dual feasibility problem's bounds)
+template <class T>
+__global__ void k_zero_finite(long n, T *v) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride)
+    if (isfinite((double)v[i])) v[i] = T(0);
+}
+
+template <class T, class M>
+void Solve<T, M>::polish_init(const Solve &main, int mode) {
+  Dev<T> &d = d_;
+  const Dev<T> &md = main.d_;
+  const int n = d.n, m = d.m;
+  const int cur = main.final_count_ & 1;  // main's current iterate at termination
+  auto copy = [&](T *dst, const T *src, int k) {
+    if (k) PDLP_CUDA(cudaMemcpyAsync(dst, src, (size_t)k * sizeof(T), cudaMemcpyDeviceToDevice, st_));
+  };
+  auto zero = [&](T *p, int k) {
+    if (k) PDLP_CUDA(cudaMemsetAsync(p, 0, (size_t)k * sizeof(T), st_));
+  };
+  d.polish = mode;
+  if (mode == 1) {
+    // objective 0 (and no objective constant, as the reference's polish state);
+    // primal iterates from the solve, dual iterates 0
+    zero((T *)d.c, n);
+    d.c_obj = md.c;
+    d.c0 = 0.0;
+    copy(d.x0, md.x0, n);
+    copy(d.x[0], md.x[cur], n);
+    copy(d.xhat, md.xhat, n);
+    copy(d.xref, md.xref, n);
+    T *const ys[] = {d.y0, d.y[0], d.y[1], d.yhat};
+    for (T *p : ys) zero(p, m);
+    zero(d.lam, n);
+  } else {
+    // finite bounds 0; the dual objective keeps the solve's finite bounds and
+    // primal point; dual iterates and dual slack from the solve, primal 0
+    const int gn = grid_for(n), gm = grid_for(m);
+    if (n) {
+      k_zero_finite<T><<<gn, kThreads, 0, st_>>>(n, (T *)d.lv);
+      k_zero_finite<T><<<gn, kThreads, 0, st_>>>(n, (T *)d.uv);
+    }
+    if (m) {
+      k_zero_finite<T><<<gm, kThreads, 0, st_>>>(m, (T *)d.lc);
+      k_zero_finite<T><<<gm, kThreads, 0, st_>>>(m, (T *)d.uc);
+    }
+    PDLP_LAUNCH_CHECK();
+    launches_ += 4;
+    d.lcf = md.lcf;
+    d.ucf = md.ucf;
+    d.x_obj = md.xhat;
+    copy(d.y0, md.y0, m);
+    copy(d.y[0], md.y[cur], m);
+    copy(d.yhat, md.yhat, m);
+    copy(d.lam, md.lam, n);
+    T *const xs[] = {d.x0, d.x[0], d.x[1], d.xhat, d.xref};
+    for (T *p : xs) zero(p, n);
+  }
+  Ctl c;
+  read_ctl(c);
+  c.fixed_point_error = c.initial_fixed_point_error = c.last_trial_fixed_point_error = INFINITY;
+  c.pw_error_sum = c.pw_last_error = 0.0;
+  c.best_gap = INFINITY;
+  PDLP_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
+  PDLP_CUDA(cudaStreamSynchronize(st_));
+}
+
+template <class T, class M>
+void Solve<T, M>::adopt_polish(const Solve &ps, int mode) {
+  Dev<T> &d = d_;
+  Ctl c, pc;
+  read_ctl(c);
+  ps.read_ctl(pc);
+  if (mode == 1) {
+    if (d.n)
+      PDLP_CUDA(cudaMemcpyAsync(d.xhat, ps.d_.xhat, (size_t)d.n * sizeof(T),
+                                cudaMemcpyDeviceToDevice, st_));
+    c.abs_primal_res = pc.abs_primal_res;
+    c.rel_primal_res = pc.rel_primal_res;
+    c.primal_obj = pc.primal_obj;
+  } else {
+    if (d.m)
+      PDLP_CUDA(cudaMemcpyAsync(d.yhat, ps.d_.yhat, (size_t)d.m * sizeof(T),
+                                cudaMemcpyDeviceToDevice, st_));
+    c.abs_dual_res = pc.abs_dual_res;
+    c.rel_dual_res = pc.rel_dual_res;
+    c.dual_obj = pc.dual_obj;
+  }
+  PDLP_CUDA(cudaMemcpyAsync(d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
+  PDLP_CUDA(cudaStreamSynchronize(st_));
+}
+
+template <class T, class M>
+void Solve<T, M>::finish_polish() {
+  Ctl c;
+  read_ctl(c);
+  c.gap = fabs(c.primal_obj - c.dual_obj);
+  c.rel_gap = c.gap / (1.0 + fabs(c.primal_obj) + fabs(c.dual_obj));
+  PDLP_CUDA(cudaMemcpyAsync(d_.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st_));
+  PDLP_CUDA(cudaStreamSynchronize(st_));
+}
+
+template <class T, class M>
+Kkt Solve<T, M>::last_kkt() const {
+  Ctl c;
+  read_ctl(c);
+  return Kkt{c.abs_primal_res, c.rel_primal_res, c.abs_dual_res, c.rel_dual_res,
+             c.primal_obj,     c.dual_obj,       c.gap,          c.rel_gap};
 }
 
 template <class T, class M>

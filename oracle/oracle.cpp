@@ -646,6 +646,159 @@ struct Solver {
     cum_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
 
+  // ----------------------------------------------------- feasibility polishing
+  // reference src/pdlp_core_op.cu:861-1360, src/utils.cu:1015-1040, :1110-1229
+  int polish_mode = 0;  // 1: primal feasibility problem, 2: dual
+  double feas_time = 0.0;
+  int feas_iter = 0;
+
+  // reference initialize_primal / initialize_dual_feas_polish_state
+  void setup_polish(int mode, double w0) {
+    polish_mode = mode;
+    auto zero = [](vec &v) { std::fill(v.begin(), v.end(), 0.0); };
+    auto zero_finite = [](vec &v) {
+      for (double &a : v)
+        if (std::isfinite(a)) a = 0.0;
+    };
+    if (mode == 1) {
+      zero(c);
+      c0 = 0.0;  // the reference's primal polish state drops the objective constant
+      zero(y0); zero(y); zero(yhat); zero(yref); zero(dprod);
+    } else {
+      zero_finite(lc); zero_finite(uc); zero_finite(lv); zero_finite(uv);
+      zero(lcf); zero(ucf); zero(lvf); zero(uvf);
+      zero(x0); zero(x); zero(xhat); zero(xref); zero(pprod);
+    }
+    if (mode == 1) zero(lam);
+    zero(pslack); zero(dres); zero(pres); zero(dx); zero(dy);
+    pw_err_sum = 0.0;
+    pw_last_err = 0.0;
+    fpe = init_fpe = last_fpe = INFINITY;
+    omega = best_omega = w0;
+    is_major = false;
+    total = inner = 0;
+    reason = TERMINATION_REASON_UNSPECIFIED;
+    cum_time = 0.0;
+    best_gap = INFINITY;
+    if (mode == 1) rel_d = abs_d = rel_gap = gap = 0.0;
+    else rel_p = abs_p = rel_gap = gap = 0.0;
+  }
+
+  // reference compute_primal_feas_polish_residual / compute_dual_...
+  void polish_residual(const Solver &ori) {
+    if (polish_mode == 1) {
+      spmv(A, xhat.data(), pprod.data());
+#pragma omp parallel for schedule(static)
+      for (int i = 0; i < m; ++i) {
+        double cl = std::fmax(lc[i], std::fmin(pprod[i], uc[i]));
+        pres[i] = (pprod[i] - cl) * Dr[i];
+      }
+      abs_p = norm(pres) / cb;
+      rel_p = abs_p / (1.0 + bnorm);
+      pobj = dot(ori.c, xhat) / (cb * ob) + c0;
+    } else {
+      spmv(AT, yhat.data(), dprod.data());
+#pragma omp parallel for schedule(static)
+      for (int j = 0; j < n; ++j) dres[j] = (c[j] - dprod[j] - lam[j]) * Dc[j];
+#pragma omp parallel for schedule(static)
+      for (int i = 0; i < m; ++i)
+        pslack[i] = std::fmax(yhat[i], 0.0) * ori.lcf[i] + std::fmin(yhat[i], 0.0) * ori.ucf[i];
+      abs_d = norm(dres) / ob;
+      rel_d = abs_d / (1.0 + cnorm);
+      double base = dot(lam, ori.xhat);
+      dobj = (base + vsum(pslack)) / (cb * ob) + c0;
+    }
+  }
+
+  // reference src/utils.cu:1015-1039
+  void polish_termination() {
+    const auto &tc = prm.termination_criteria;
+    double r = polish_mode == 1 ? rel_p : rel_d;
+    if (r <= tc.eps_feas_polish_relative) reason = TERMINATION_REASON_FEAS_POLISH_SUCCESS;
+    else if (total >= tc.iteration_limit) reason = TERMINATION_REASON_ITERATION_LIMIT;
+    else if (cum_time >= tc.time_sec_limit) reason = TERMINATION_REASON_TIME_LIMIT;
+  }
+
+  // reference primal_feasibility_polish / dual_feasibility_polish: the loop
+  // of the solve with one-sided restarts and fixed-point error; like the
+  // reference, the iteration in progress completes after termination
+  void polish_loop(const Solver &ori) {
+    int F = prm.termination_evaluation_frequency;
+    auto t0 = std::chrono::steady_clock::now();
+    bool restart = false;
+    while (reason == TERMINATION_REASON_UNSPECIFIED) {
+      if (is_major || total == 0 || total % print_frequency(total) == 0) {
+        polish_residual(ori);
+        cum_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        polish_termination();
+      }
+      if (is_major || total == 0) {
+        restart = should_restart();
+        if (restart) {  // reference perform_primal_restart / perform_dual_restart
+          if (polish_mode == 1) x0 = x = xhat;
+          else y0 = y = yhat;
+          inner = 0;
+          last_fpe = INFINITY;
+        }
+      }
+      is_major = ((total + 1) % F) == 0;
+      bool major_kernel = is_major || ((total + 2) % print_frequency(total + 2)) == 0;
+      primal_step(major_kernel);
+      dual_step(major_kernel);
+      if (is_major || restart) {  // reference compute_primal/dual_fixed_point_error
+        if (polish_mode == 1) {
+#pragma omp parallel for schedule(static)
+          for (int j = 0; j < n; ++j) dx[j] = xref[j] - x[j];
+          double pn = nrm2(dx);
+          fpe = pn * pn * omega;
+        } else {
+#pragma omp parallel for schedule(static)
+          for (int i = 0; i < m; ++i) dy[i] = yref[i] - y[i];
+          double dn = nrm2(dy);
+          fpe = dn * dn / omega;
+        }
+        if (restart) {
+          init_fpe = fpe;
+          restart = false;
+        }
+      }
+      halpern();
+      ++inner;
+      ++total;
+    }
+  }
+
+  // reference feasibility_polish (src/pdlp_core_op.cu:862-930)
+  void feasibility_polish() {
+    auto t0 = std::chrono::steady_clock::now();
+    const double eps = prm.termination_criteria.eps_feas_polish_relative;
+    if (rel_p < eps && rel_d < eps) return;
+    double w0 = prm.bound_objective_rescaling ? 1.0 : (cnorm + 1.0) / (bnorm + 1.0);
+    Solver ps = *this;
+    ps.setup_polish(1, w0);
+    ps.polish_loop(*this);
+    if (ps.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+      xhat = ps.xhat;
+      abs_p = ps.abs_p;
+      rel_p = ps.rel_p;
+      pobj = ps.pobj;
+    }
+    feas_iter += ps.total - 1;
+    Solver ds = *this;
+    ds.setup_polish(2, w0);
+    ds.polish_loop(*this);
+    if (ds.reason == TERMINATION_REASON_FEAS_POLISH_SUCCESS) {
+      yhat = ds.yhat;
+      abs_d = ds.abs_d;
+      rel_d = ds.rel_d;
+      dobj = ds.dobj;
+    }
+    feas_iter += ds.total - 1;
+    gap = std::fabs(pobj - dobj);
+    rel_gap = gap / (1.0 + std::fabs(pobj) + std::fabs(dobj));
+    feas_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
   // reference src/pdlp_core_op.cu:789-859
   cupdlpx_result_t *result(const lp_problem_t *p) {
     auto *r = (cupdlpx_result_t *)calloc(1, sizeof(cupdlpx_result_t));
@@ -680,6 +833,8 @@ struct Solver {
     r->primal_ray_linear_objective = pray_obj;
     r->dual_ray_objective = dray_obj;
     r->termination_reason = reason;
+    r->feasibility_polishing_time = feas_time;
+    r->feasibility_iteration = feas_iter;
     return r;
   }
 };
@@ -752,6 +907,10 @@ cupdlpx_result_t *oracle_solve(const lp_problem_t *prob,
   s.init(prob);
   s.init_step();
   s.run(trace, trace_cap, trace_len);
+  // reference src/solver.cu:111-115
+  if (local.feasibility_polishing && s.reason != TERMINATION_REASON_DUAL_INFEASIBLE &&
+      s.reason != TERMINATION_REASON_PRIMAL_INFEASIBLE)
+    s.feasibility_polish();
   return s.result(prob);
 }
 
