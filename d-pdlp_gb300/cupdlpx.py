@@ -266,6 +266,14 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_device_problem_time_kernels_prec.restype = C.c_int
     lib.pdlp_device_problem_time_kernels_prec.argtypes = [C.c_void_p, C.POINTER(PdhgParameters),
                                                           C.c_int, C.c_int, _dp]
+    lib.pdlp_problem_wire_size.restype = C.c_longlong
+    lib.pdlp_problem_wire_size.argtypes = [P]
+    lib.pdlp_problem_serialize.restype = C.c_longlong
+    lib.pdlp_problem_serialize.argtypes = [P, C.c_void_p, C.c_longlong]
+    lib.pdlp_problem_deserialize.restype = P
+    lib.pdlp_problem_deserialize.argtypes = [C.c_void_p, C.c_longlong]
+    lib.pdlp_server_submit_bytes.restype = C.c_longlong
+    lib.pdlp_server_submit_bytes.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong]
     lib.read_mps_file.restype = P
     lib.read_mps_file.argtypes = [C.c_char_p]
     lib.pdlp_estimate_device_bytes.restype = C.c_longlong
@@ -414,6 +422,22 @@ class Problem:
     def arrays(self) -> dict:
         return problem_arrays(self.ptr)
 
+    def to_bytes(self) -> bytes:
+        """The problem in the binary request format (pdlp_problem_serialize)."""
+        size = self._lib.pdlp_problem_wire_size(self.ptr)
+        buf = C.create_string_buffer(max(int(size), 1))
+        if self._lib.pdlp_problem_serialize(self.ptr, buf, size) != size:
+            raise RuntimeError("serialize failed")
+        return buf.raw[:size]
+
+    @classmethod
+    def from_bytes(cls, data: bytes, library: C.CDLL | None = None) -> "Problem":
+        L = library or lib()
+        ptr = L.pdlp_problem_deserialize(data, len(data))
+        if not ptr:
+            raise ValueError("malformed problem payload")
+        return cls(ptr, L)
+
     def set_start(self, x=None, y=None):
         conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
         xs, ys = conv(x), conv(y)
@@ -545,6 +569,12 @@ class Server:
         rid = self._lib.pdlp_server_submit(self.handle, problem.ptr)
         if rid < 0:
             raise RuntimeError("submit failed")
+        return rid
+
+    def submit_bytes(self, payload: bytes) -> int:
+        rid = self._lib.pdlp_server_submit_bytes(self.handle, payload, len(payload))
+        if rid < 0:
+            raise RuntimeError("submit failed: malformed payload")
         return rid
 
     def wait(self, rid: int) -> tuple[dict, dict]:

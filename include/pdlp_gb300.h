@@ -2,8 +2,11 @@
  * pdlp_gb300.h -- additions of the GB300 solver beyond the reference C API.
  *
  * Nothing here replaces a reference entry point; these are new, namespaced
- * functions (diagnostics, seeded problem generators, and the device-level
- * hooks the parity tests call).  All take plain host pointers and sizes.
+ * functions: solve diagnostics and precision options, problems resident in
+ * HBM, the batch / serving runtime, the binary problem format, seeded
+ * problem generators, and the device-level hooks the parity tests call.
+ * They take plain pointers and sizes (host memory unless a function says
+ * device).
  * Errors: functions returning int give 0 on success and a negative code on
  * failure; pdlp_last_error() then describes the failure of the calling thread.
  */
@@ -187,6 +190,22 @@ int pdlp_batch_solve(const lp_problem_t *const *probs, int count,
                      const pdhg_parameters_t *params, const pdlp_options_t *opts,
                      int workers, long long mem_budget_bytes,
                      cupdlpx_result_t **results, pdlp_batch_info_t *info);
+
+/* ---- binary problem format ----------------------------------------------
+ * The byte layout of the reference's serialize_lp_problem_to_ptr
+ * (src/distribution_utils.cu:279-405), for request payloads and stored
+ * instances: int32 n, m, nnz; float64 objective constant; float64 c[n],
+ * lv[n], uv[n], lc[m], uc[m]; int32 row_ptr[m+1], col[nnz]; float64
+ * val[nnz]; int32 has_primal_start, has_dual_start; then the start vectors
+ * present.  Host byte order, packed. */
+long long pdlp_problem_wire_size(const lp_problem_t *lp);
+/* Write lp into buf (capacity bytes); returns the bytes written or -1. */
+long long pdlp_problem_serialize(const lp_problem_t *lp, void *buf, long long capacity);
+/* Read a payload of `length` bytes; NULL when it is truncated or its CSR is
+ * inconsistent.  Free with lp_problem_free. */
+lp_problem_t *pdlp_problem_deserialize(const void *buf, long long length);
+/* pdlp_server_submit of a payload in that format. */
+long long pdlp_server_submit_bytes(pdlp_server_t *s, const void *buf, long long length);
 
 /* Return the device memory cached by the library's pool. */
 void pdlp_release_pooled_memory(void);

@@ -105,3 +105,13 @@ def test_failed_request_reports_error_and_others_finish():
     res, info = cp.batch_solve([good[0], bad, good[1]], p, workers=2)
     assert info["failed"] == 1
     assert res[1] is None and res[0] is not None and res[2] is not None
+
+
+def test_wire_payloads_solve_like_problems():
+    lps = _mixed_lps(3, seed0=950)
+    p = _params()
+    with cp.Server(p, workers=2) as srv:
+        ids = [srv.submit_bytes(lp.to_bytes()) for lp in lps]
+        got = [srv.wait(i)[0] for i in ids]
+    for lp, g in zip(lps, got):
+        _same(cp.solve(lp, p).result, g)
