@@ -391,6 +391,11 @@ def run_kernels_only(args, cp):
                                         "eval_A": ms[2], "eval_AT": ms[3]}}))
 
 
+PRECISIONS = {"fp32": 1, "fp32m": 2, "fp64": 0}
+DTYPES = {"fp32": "f32 iterates + f64 KKT/refinement",
+          "fp32m": "f32 matrix/SpMV + f64 iterates/KKT/refinement", "fp64": "f64"}
+
+
 def batch_shapes(count, seed0):
     """(m, n, nnz, seed) of the batch workload's LPs."""
     import numpy as np
@@ -420,21 +425,36 @@ def run_batch(args, cp):
     lps = generate_parallel(cp, shapes)
     nnz_total = sum(sh[2] for sh in shapes)
     params = params_for(cp, args.eps)
+    prec = PRECISIONS[args.precision]
     for _ in range(args.warmup):
-        cp.batch_solve(lps, params, workers=args.workers)
+        cp.batch_solve(lps, params, precision=prec, workers=args.workers)
     vals, iters = [], 0
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
-            res, info = cp.batch_solve(lps, params, workers=args.workers)
+            res, info = cp.batch_solve(lps, params, precision=prec, workers=args.workers)
             vals.append(info["lps_per_second"])
             iters = info["iterations"]
             failed = info["failed"]
     clocks = clk.summary()
+    statuses = sorted({r["status"] for r in res if r is not None})
+    worst = max(max(r["relative_primal_residual"], r["relative_dual_residual"],
+                    r["relative_objective_gap"]) for r in res if r is not None)
+    fp64_batch = None
+    if prec != cp.PRECISION_FP64:
+        r64, i64 = cp.batch_solve(lps, params, workers=args.workers)
+        fp64_batch = {"lps_per_second": round(i64["lps_per_second"], 2),
+                      "iterations": i64["iterations"]}
     # the same LPs one after another (our FP64 path, one stream)
     t0 = time.perf_counter()
     seq = [cp.solve(lp, params).result for lp in lps]
     t_seq = time.perf_counter() - t0
-    same = all(a is not None and a["total_count"] == b["total_count"] for a, b in zip(res, seq))
+    if prec == cp.PRECISION_FP64:
+        same = all(a is not None and a["total_count"] == b["total_count"]
+                   for a, b in zip(res, seq))
+    else:  # FP32 + refinement against the FP64 solves: objectives within eps
+        same = all(a is not None and abs(a["primal_objective_value"] - b["primal_objective_value"])
+                   <= 10 * args.eps * (1 + abs(b["primal_objective_value"]))
+                   for a, b in zip(res, seq))
     value = statistics.mean(vals)
     cpu = None
     if not args.no_cpu_baseline:
@@ -453,9 +473,11 @@ def run_batch(args, cp):
     line = {
         "metric": "batched LPs/s", "value": round(value, 2), "unit": "LPs/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(count / value * 1e3, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": args.workload, "description": w["desc"], "lps": count,
+                   "precision": args.precision,
                    "nnz_total": nnz_total, "workers": args.workers, "eps": args.eps,
                    "l2": "inputs larger than L2; no flush needed"},
         "e2e": {"value": round(value, 2), "unit": "LPs/s",
@@ -466,7 +488,9 @@ def run_batch(args, cp):
         "sequential": {"lps_per_second": round(count / t_seq, 2), "seconds": round(t_seq, 2),
                        "api": "solve_lp_problem, one LP after another"},
         "batch": {"iterations": iters, "failed": failed, "max_concurrent": info["max_concurrent"],
+                  "statuses": statuses, "worst_relative_kkt": worst,
                   "results_match_sequential": same},
+        "fp64_batched": fp64_batch,
         "clocks": clocks,
     }
     if cpu:
@@ -495,9 +519,10 @@ def run_serve(args, cp):
             int(rng.integers(w["pool_small"]))
         arrivals.append((t, idx))
     params = params_for(cp, args.eps)
+    prec = PRECISIONS[args.precision]
     import threading
     lat, done_t = [None] * len(arrivals), [None] * len(arrivals)
-    with cp.Server(params, workers=args.workers) as srv:
+    with cp.Server(params, precision=prec, workers=args.workers) as srv:
         ids = [None] * len(arrivals)
         t0 = time.perf_counter()
 
@@ -526,8 +551,10 @@ def run_serve(args, cp):
         "metric": "served LPs/s; p50/p99 latency", "value": round(len(arrivals) / total, 2),
         "unit": "LPs/s", "n_gpus": 1, "steps": 1, "warmup": 0,
         "ms_per_step": round(total * 1e3, 1), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, no dataset)",
+        "vs_baseline": None, "dtype": DTYPES[args.precision],
+        "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": args.workload, "description": w["desc"], "rate_per_s": rate,
+                   "precision": args.precision,
                    "duration_s": duration, "requests": len(arrivals), "workers": args.workers,
                    "pool": f"{w['pool_small']} batch-distribution LPs + {w['pool_large']} large",
                    "eps": args.eps},
@@ -595,9 +622,11 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-4)
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default="fp64",
+    ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default=None,
                     help="fp32: FP32 iterates + FP64 refinement; fp32m: FP32 matrix "
-                         "and SpMVs with FP64 iterates + FP64 refinement; fp64 (default): plain FP64")
+                         "and SpMVs with FP64 iterates + FP64 refinement; fp64: plain FP64 "
+                         "(default: fp64 for single solves, fp32 for the batch and serving "
+                         "workloads, as their configurations specify)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time the iteration kernels alone and exit (a short command for "
                          "profilers; prints no bench line)")
@@ -605,6 +634,9 @@ def main():
                     help="timed FP64 solves reported beside an FP32 run (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
+    if args.precision is None:
+        many = args.workload in BATCH_WORKLOADS or args.workload in SERVE_WORKLOADS
+        args.precision = "fp32" if many else "fp64"
     os.environ.setdefault("PDLP_QUIET", "1")
     rank, world, local = rank_info()
     if world > 1:
