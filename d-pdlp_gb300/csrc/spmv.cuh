@@ -17,8 +17,9 @@
 //                  runs with all 32 lanes.  Few long rows: a group of G lanes
 //                  per row (G = 256 / rows, power of two, at most 32); a tile
 //                  with one row uses the whole block;
-//   * long row   : a row with more than TILE non-zeros is cut into chunks, one
-//                  block each; the last block to finish (atomic ticket) sums
+//   * long row   : a row with more than TILE non-zeros is cut into chunks (up
+//                  to 8 tiles long), one block each, folded in passes of TILE
+//                  non-zeros; the last block to finish (atomic ticket) sums
 //                  the chunk partials in chunk order and runs the epilogue.
 // Every sum has a fixed order for a given plan, so results are bitwise
 // reproducible run to run.  The epilogue of row r runs once, in one thread,
@@ -46,20 +47,22 @@ struct SpmvPlan {
 };
 
 // Host: cut rows into tiles.  `ptr` is the host copy of the row pointer.
+// Rows longer than `tile` are cut into chunks of `chunk` (>= tile) non-zeros.
 inline void build_plan_host(int rows, const int *ptr, int tile,
-                            std::vector<int4> &blk, std::vector<int2> &lrow) {
+                            std::vector<int4> &blk, std::vector<int2> &lrow, int chunk = 0) {
   blk.clear();
   lrow.clear();
+  if (chunk < tile) chunk = tile;
   int r = 0;
   while (r < rows) {
     int len = ptr[r + 1] - ptr[r];
     if (len > tile) {
-      int nch = (len + tile - 1) / tile;
+      int nch = (len + chunk - 1) / chunk;
       int lid = (int)lrow.size();
       lrow.push_back(make_int2((int)blk.size(), nch));
       for (int c = 0; c < nch; ++c) {
-        int k0 = ptr[r] + c * tile;
-        int k1 = k0 + tile < ptr[r + 1] ? k0 + tile : ptr[r + 1];
+        int k0 = ptr[r] + c * chunk;
+        int k1 = k0 + chunk < ptr[r + 1] ? k0 + chunk : ptr[r + 1];
         blk.push_back(make_int4(r, -(lid + 1), k0, k1));
       }
       ++r;
@@ -188,12 +191,13 @@ __global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
     // warp.  Rows of up to ~10^5 terms with cancellation keep every sum across
     // threads, warps and chunks in FP64.
     A s = A(0);
-    {
+    // the chunk (any length) in passes of IPT elements per thread
+    for (int base = 0; base < len; base += IPT * kThreads) {
       int cidx[IPT];
       T v[IPT], xg[IPT];
 #pragma unroll
       for (int u = 0; u < IPT; ++u) {
-        int i = threadIdx.x + u * kThreads;
+        int i = base + threadIdx.x + u * kThreads;
         if (i < len) {
           cidx[u] = ld_stream(col + k0 + i);
           v[u] = ld_stream(val + k0 + i);
@@ -201,10 +205,10 @@ __global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
       }
 #pragma unroll
       for (int u = 0; u < IPT; ++u)
-        if (threadIdx.x + u * kThreads < len) xg[u] = epi.gather(cidx[u]);
+        if (base + threadIdx.x + u * kThreads < len) xg[u] = epi.gather(cidx[u]);
 #pragma unroll
       for (int u = 0; u < IPT; ++u)
-        if (threadIdx.x + u * kThreads < len) s = fma((A)v[u], (A)xg[u], s);
+        if (base + threadIdx.x + u * kThreads < len) s = fma((A)v[u], (A)xg[u], s);
     }
     double *tp = reinterpret_cast<double *>(sv);
     tp[threadIdx.x] = (double)s;
