@@ -25,10 +25,13 @@ struct PlainEpi {
 
 }  // namespace pdlp
 
-extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *col_ind,
-                             const double *vals, const double *x, double *y, int tile) {
+extern "C" int pdlp_gpu_spmv_variant(int rows, int cols, const int *row_ptr,
+                                     const int *col_ind, const double *vals, const double *x,
+                                     double *y, int tile, int variant) {
   using namespace pdlp;
-  if (rows < 0 || cols < 0 || !row_ptr || (tile != 512 && tile != 2048)) return -1;
+  if (rows < 0 || cols < 0 || !row_ptr || (tile != 512 && tile != 1024 && tile != 2048))
+    return -1;
+  if (variant < 0 || variant > 2 || (variant > 0 && tile != 1024)) return -1;
   const int nnz = row_ptr[rows];
   for (int r = 0; r < rows; ++r)
     if (row_ptr[r] > row_ptr[r + 1]) return -1;
@@ -49,8 +52,9 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
       return q;
     };
     int *dptr = (int *)take(((size_t)rows + 1) * 4);
-    int *dcol = (int *)take((size_t)nnz * 4 + 4);
-    double *dval = (double *)take((size_t)nnz * 8 + 8);
+    // variant 2: column and value arrays 4 and 8 bytes past a 16-byte boundary
+    int *dcol = (int *)take((size_t)nnz * 4 + 4) + (variant == 2 ? 1 : 0);
+    double *dval = (double *)take((size_t)nnz * 8 + 8) + (variant == 2 ? 1 : 0);
     double *dx = (double *)take((size_t)cols * 8 + 8);
     double *dy = (double *)take((size_t)rows * 8 + 8);
     SpmvPlan plan;
@@ -58,6 +62,7 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
     plan.nblk = (int)blk.size();
     plan.nlong = (int)lr.size();
     plan.tile = tile;
+    plan.direct = variant > 0;
     plan.blk = (int4 *)take(blk.size() * 16 + 16);
     plan.lrow = (int2 *)take(lr.size() * 8 + 8);
     plan.lcnt = (unsigned *)take(lr.size() * 4 + 4);
@@ -79,6 +84,12 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
       if (tile == 2048)
         spmv_fused<2048, PlainEpi><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan, nullptr,
                                                             nullptr, e);
+      else if (tile == 1024 && plan.direct)
+        spmv_fused<1024, PlainEpi, true><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan,
+                                                                  nullptr, nullptr, e);
+      else if (tile == 1024)
+        spmv_fused<1024, PlainEpi><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan, nullptr,
+                                                            nullptr, e);
       else
         spmv_fused<512, PlainEpi><<<plan.nblk, kThreads>>>(dptr, dcol, dval, plan, nullptr,
                                                            nullptr, e);
@@ -92,4 +103,10 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
     fprintf(stderr, "[cupdlpx-gb300] pdlp_gpu_spmv: %s\n", e.what());
     return -2;
   }
+}
+
+extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *col_ind,
+                             const double *vals, const double *x, double *y, int tile) {
+  if (tile != 512 && tile != 2048) return -1;
+  return pdlp_gpu_spmv_variant(rows, cols, row_ptr, col_ind, vals, x, y, tile, 0);
 }

@@ -356,6 +356,9 @@ void launch_spmv(const DevCsrT<V> &M, const Epi &epi, double *part, double *lpar
   if (M.plan.tile == 2048)
     spmv_fused<2048, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
                                                              part, lpart, epi);
+  else if (M.plan.tile == 1024 && M.plan.direct)
+    spmv_fused<1024, Epi, true><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
+                                                                   part, lpart, epi);
   else if (M.plan.tile == 1024)
     spmv_fused<1024, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,
                                                              part, lpart, epi);

@@ -212,6 +212,10 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
     M.plan.nblk = (int)blk.size();
     M.plan.nlong = (int)lr.size();
     M.plan.tile = P->tile;
+    // register-path kernel variant for matrices of short rows of 16+ non-zeros
+    // (tiles of 1024 only); PDLP_SPMV_DIRECT=0/1 overrides the rule
+    M.plan.direct = P->tile == 1024 && plan_direct(blk, nnz);
+    if (const char *e = getenv("PDLP_SPMV_DIRECT")) M.plan.direct = P->tile == 1024 && atoi(e) != 0;
     M.plan.blk = ar.take<int4>(blk.size());
     M.plan.lrow = ar.take<int2>(lr.size());
     if (!blk.empty())

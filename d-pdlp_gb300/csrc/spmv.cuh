@@ -16,7 +16,10 @@
 //                  row adds its 1-3 segment partials -- every FP64 instruction
 //                  runs with all 32 lanes.  Few long rows: a group of G lanes
 //                  per row (G = 256 / rows, power of two, at most 32); a tile
-//                  with one row uses the whole block;
+//                  with one row uses the whole block.  In the DIRECT variant
+//                  (chosen per matrix), short rows of 16 or more non-zeros
+//                  skip the staging: each lane loads, gathers and folds an
+//                  aligned group of 4 elements in registers;
 //   * long row   : a row with more than TILE non-zeros is cut into chunks (up
 //                  to 8 tiles long), one block each, folded in passes of TILE
 //                  non-zeros; the last block to finish (atomic ticket) sums
@@ -40,6 +43,7 @@ constexpr int kMaxRowsPerTile = 1024;
 
 struct SpmvPlan {
   int rows = 0, nblk = 0, nlong = 0, tile = 0;
+  int direct = 0;             // launch the register-path variant (see plan_direct)
   int4 *blk = nullptr;        // {r0, r1 | -(long_id+1), k0, k1}
   int2 *lrow = nullptr;       // per long row {first block, chunk count}
   unsigned *lcnt = nullptr;   // per long row arrival counter (kept at 0)
@@ -72,6 +76,27 @@ inline void build_plan_host(int rows, const int *ptr, int tile,
       blk.push_back(make_int4(r0, r, k0, ptr[r]));
     }
   }
+}
+
+// Light tiles whose rows hold at least this many non-zeros on average take
+// the register path (4-element groups per lane) in the DIRECT variant of the
+// kernel; shorter rows are staged through shared memory.
+constexpr int kDirectMinAvg = 16;
+
+// Host: whether a matrix should run the register-path variant -- when at least
+// half of its non-zeros sit in short-row tiles of kDirectMinAvg or more
+// non-zeros per row.  Measured per step with tiles of 1024 (FP64): the
+// power-law LP's A (m = 1M, rows of ~20) 0.151 -> 0.135 ms; a random LP's A
+// (m = 200k, rows of ~25) 0.049 ms either way; rows of ~10 (that LP's
+// transpose) 0.047 -> 0.051 ms and rows of 1-4 0.153 -> 0.170 ms, so those
+// stay on the staged kernel at 6 blocks per SM.
+inline bool plan_direct(const std::vector<int4> &blk, long nnz) {
+  long in = 0;
+  for (const int4 &b : blk) {
+    const int R = b.y - b.x, len = b.w - b.z;
+    if (b.y >= 0 && R > 1 && len <= 64 * R && len >= kDirectMinAvg * R) in += len;
+  }
+  return nnz > 0 && 2 * in >= nnz;
 }
 
 template <class T>
@@ -122,9 +147,9 @@ __device__ __forceinline__ void block_reduce_fields(double (&acc)[NF > 0 ? NF : 
 // scalars that need a division (step sizes, Halpern weight) are formed once
 // per block by thread 0.
 // Shared-memory swizzle for the staged (value, x) pairs: phase 1 writes
-// consecutive elements per lane, the stream phase reads 8 consecutive elements
-// per lane (lane stride 8); XOR-ing the low 3 bits with higher index bits makes
-// both patterns bank-conflict free for 4- and 8-byte elements.
+// consecutive elements per lane, the staged stream phase reads 8 consecutive
+// elements per lane (lane stride 8); XOR-ing the low 3 bits with higher index
+// bits makes both patterns bank-conflict free for 4- and 8-byte elements.
 template <class T>
 __device__ __forceinline__ int swz(int i) {
   return i ^ ((i >> (sizeof(T) == 8 ? 4 : 5)) & 7);
@@ -150,14 +175,16 @@ struct pre_of<E, true> {
 // latency-bound (dependent col -> gather -> FMA chains, per-row vector loads),
 // so residency pays: 6 blocks of 256 threads (40 registers) for tiles of up
 // to 1024 non-zeros.  2048-element tiles need their registers (the long-row
-// path keeps 8 loads per thread in flight) and run at 4 blocks.
-template <int TILE>
+// path keeps 8 loads per thread in flight) and run at 4 blocks.  The
+// register-path variant holds a group's columns and values across the first
+// barrier and runs at 5 blocks (48 registers, no spills).
+template <int TILE, bool DIRECT = false>
 constexpr int spmv_min_blocks() {
-  return TILE >= 2048 ? 1 : 6;
+  return TILE >= 2048 ? 1 : DIRECT ? 5 : 6;
 }
 
-template <int TILE, class Epi>
-__global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
+template <int TILE, class Epi, bool DIRECT = false>
+__global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE, DIRECT>())
     spmv_fused(const int *__restrict__ ptr, const int *__restrict__ col,
                const typename Epi::val_t *__restrict__ val, SpmvPlan plan,
                double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
@@ -165,10 +192,10 @@ __global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
   using A = typename Epi::acc_t;
   constexpr int NF = Epi::NF;
   constexpr int IPT = TILE / kThreads;
-  constexpr int SEG = 8;  // elements per lane in the stream phase
-  __shared__ __align__(16) T sv[TILE];  // values; stream-phase segment partials;
-                                         // chunk partials of a long row (as doubles)
-  __shared__ T sx[TILE];  // gathered x
+  static_assert(sizeof(A) == sizeof(T), "run partials share the value buffer");
+  __shared__ __align__(16) T sv[TILE + 8];  // values; run partials of short rows;
+                                             // chunk partials of a long row (as doubles)
+  __shared__ __align__(16) T sx[TILE];      // gathered x; start rows of short-row groups
   __shared__ int soff[kMaxRowsPerTile + 1];
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
   __shared__ double sc[4];
@@ -254,65 +281,105 @@ __global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
 
   const bool stream = R > 1 && len <= 64 * R;
   [[maybe_unused]] typename pre_of<Epi>::type pre;
-  // Phase 1: coalesced stream of values / columns, gather of x, row offsets.
-  {
-    int cidx[IPT];
-#pragma unroll
-    for (int u = 0; u < IPT; ++u) {
-      int i = threadIdx.x + u * kThreads;
-      if (i < len) {
-        cidx[u] = ld_stream(col + k0 + i);
-        sv[swz<T>(i)] = ld_stream(val + k0 + i);
-      }
-    }
-    if constexpr (has_preload<Epi>::value) {
-      if (stream && threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
-    }
-    for (int j = threadIdx.x; j <= R; j += kThreads) soff[j] = ptr[b.x + j] - k0;
-#pragma unroll
-    for (int u = 0; u < IPT; ++u) {
-      int i = threadIdx.x + u * kThreads;
-      if (i < len) sx[swz<T>(i)] = epi.gather(cidx[u]);
-    }
-  }
-  __syncthreads();
-  epi.bind(sc);
-
-  if (stream) {
-    // Stream phase: lane t folds elements [8t, 8t+8) with FMA, all lanes busy;
-    // each finished segment's partial goes to sv[swz(start)], a slot the lane
-    // has already consumed.
-    const int beg = threadIdx.x * SEG;
-    if (beg < len) {
-      const int end = beg + SEG < len ? beg + SEG : len;
-      int lo = 0, hi = R;  // row j with soff[j] <= beg < soff[j+1]
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (soff[mid] <= beg) lo = mid;
-        else hi = mid;
-      }
-      int j = lo, nb = soff[j + 1], segs = beg;
-      A s = A(0);
-      for (int e = beg; e < end; ++e) {
-        while (e == nb) {
-          if (segs < e) sv[swz<T>(segs)] = (T)s;
-          s = A(0);
-          segs = e;
-          ++j;
-          nb = soff[j + 1];
+  if (DIRECT && stream && len >= kDirectMinAvg * R) {
+    // Register path, rows of kDirectMinAvg or more non-zeros on average: lane
+    // g owns the aligned group [kb + 4g, kb + 4g + 4) of the matrix arrays
+    // (kb = k0 rounded down to a multiple of 4; elements outside [k0, k0 +
+    // len) are skipped).  It loads the group with 16-byte vector loads (scalar
+    // loads for a partial group or arrays off 16-byte boundaries) straight
+    // into registers, gathers x and folds it with FMA; only the row offsets,
+    // the start row of each group and the partial of each run (a row's
+    // elements inside one group) pass through shared memory, and the first
+    // barrier waits for row offsets only, not for the matrix stream.
+    constexpr int GRP = 4;
+    A *runp = reinterpret_cast<A *>(sv);      // run partials by position - kb
+    int *srow = reinterpret_cast<int *>(sx);  // row holding position GRP * g
+    const int k1 = k0 + len, kb = k0 & ~(GRP - 1);
+    const int ngrp = (k1 - kb + GRP - 1) / GRP;
+    const bool vec =
+        ((reinterpret_cast<uintptr_t>(col) | reinterpret_cast<uintptr_t>(val)) & 15) == 0;
+    auto load_group = [&](int g, int (&c)[GRP], T (&v)[GRP]) {
+      const int base = kb + GRP * g;
+      if (vec && base >= k0 && base + GRP <= k1) {
+        const int4 c4 = __ldcs(reinterpret_cast<const int4 *>(col + base));
+        c[0] = c4.x; c[1] = c4.y; c[2] = c4.z; c[3] = c4.w;
+        if constexpr (sizeof(T) == 8) {
+          const double2 v0 = __ldcs(reinterpret_cast<const double2 *>(val + base));
+          const double2 v1 = __ldcs(reinterpret_cast<const double2 *>(val + base) + 1);
+          v[0] = v0.x; v[1] = v0.y; v[2] = v1.x; v[3] = v1.y;
+        } else {
+          const float4 v4 = __ldcs(reinterpret_cast<const float4 *>(val + base));
+          v[0] = v4.x; v[1] = v4.y; v[2] = v4.z; v[3] = v4.w;
         }
-        s = fma((A)sv[swz<T>(e)], (A)sx[swz<T>(e)], s);
+      } else {
+#pragma unroll
+        for (int u = 0; u < GRP; ++u) {
+          const int e = base + u;
+          if (e >= k0 && e < k1) {
+            c[u] = ld_stream(col + e);
+            v[u] = ld_stream(val + e);
+          }
+        }
       }
-      sv[swz<T>(segs)] = (T)s;
+    };
+    auto fold_group = [&](int g, const int (&c)[GRP], const T (&v)[GRP]) {
+      const int base = GRP * g;  // relative to kb
+      const int lo = (k0 - kb) > base ? (k0 - kb) : base;
+      const int hi = (k1 - kb) < base + GRP ? (k1 - kb) : base + GRP;
+      T xg[GRP];
+#pragma unroll
+      for (int u = 0; u < GRP; ++u)
+        if (base + u >= lo && base + u < hi) xg[u] = epi.gather(c[u]);
+      // group 0 may start before the tile: begin at row 0 and step over
+      // empty rows; later groups start inside the row that srow names
+      int j = g == 0 ? 0 : srow[g];
+      int nb = soff[j + 1], segs = lo;
+      A s = A(0);
+#pragma unroll
+      for (int u = 0; u < GRP; ++u) {
+        const int e = base + u;
+        if (e >= lo && e < hi) {
+          while (e == nb) {
+            if (segs < e) runp[segs] = s;
+            s = A(0);
+            segs = e;
+            ++j;
+            nb = soff[j + 1];
+          }
+          s = fma((A)v[u], (A)xg[u], s);
+        }
+      }
+      if (lo < hi) runp[segs] = s;
+    };
+
+    int c[GRP];
+    T v[GRP];
+    if ((int)threadIdx.x < ngrp) load_group(threadIdx.x, c, v);
+    if constexpr (has_preload<Epi>::value) {
+      if ((int)threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
+    }
+    for (int j = threadIdx.x; j <= R; j += kThreads) {
+      const int a = ptr[b.x + j] - kb;
+      soff[j] = a;
+      if (j < R) {
+        const int e = ptr[b.x + j + 1] - kb;
+        for (int q = (a + GRP - 1) & ~(GRP - 1); q < e; q += GRP) srow[q / GRP] = j;
+      }
     }
     __syncthreads();
-    // Row fold: segment at the row start, then one per lane boundary inside.
+    epi.bind(sc);
+    for (int g = threadIdx.x; g < ngrp; g += kThreads) {
+      if (g != (int)threadIdx.x) load_group(g, c, v);  // tiles of more than 256 groups
+      fold_group(g, c, v);
+    }
+    __syncthreads();
+    // Row fold: the run at the row start, then one per group boundary inside.
     for (int j = threadIdx.x; j < R; j += kThreads) {
       const int a = soff[j], e = soff[j + 1];
       A sum = A(0);
       if (a < e) {
-        sum = (A)sv[swz<T>(a)];
-        for (int q = (a / SEG + 1) * SEG; q < e; q += SEG) sum += (A)sv[swz<T>(q)];
+        sum = runp[a];
+        for (int q = (a & ~(GRP - 1)) + GRP; q < e; q += GRP) sum += runp[q];
       }
       if constexpr (has_preload<Epi>::value) {
         if (j == (int)threadIdx.x) epi.row_pre(b.x + j, sum, pre, acc);
@@ -322,8 +389,75 @@ __global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE>())
       }
     }
   } else {
+    // Phase 1: coalesced stream of values / columns, gather of x, row offsets.
+    {
+      int cidx[IPT];
+#pragma unroll
+      for (int u = 0; u < IPT; ++u) {
+        int i = threadIdx.x + u * kThreads;
+        if (i < len) {
+          cidx[u] = ld_stream(col + k0 + i);
+          sv[swz<T>(i)] = ld_stream(val + k0 + i);
+        }
+      }
+      if constexpr (has_preload<Epi>::value) {
+        if (stream && threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
+      }
+      for (int j = threadIdx.x; j <= R; j += kThreads) soff[j] = ptr[b.x + j] - k0;
+#pragma unroll
+      for (int u = 0; u < IPT; ++u) {
+        int i = threadIdx.x + u * kThreads;
+        if (i < len) sx[swz<T>(i)] = epi.gather(cidx[u]);
+      }
+    }
+    __syncthreads();
+    epi.bind(sc);
     const int r0 = b.x;
-    if (R == 1) {
+    if (stream) {
+      // Very short rows: lane t folds staged elements [8t, 8t+8) with FMA, all
+      // lanes busy; each finished segment's partial goes to sv[swz(start)], a
+      // slot the lane has already consumed.
+      constexpr int SEG = 8;
+      const int beg = threadIdx.x * SEG;
+      if (beg < len) {
+        const int end = beg + SEG < len ? beg + SEG : len;
+        int lo = 0, hi = R;  // row j with soff[j] <= beg < soff[j+1]
+        while (hi - lo > 1) {
+          int mid = (lo + hi) >> 1;
+          if (soff[mid] <= beg) lo = mid;
+          else hi = mid;
+        }
+        int j = lo, nb = soff[j + 1], segs = beg;
+        A s = A(0);
+        for (int e = beg; e < end; ++e) {
+          while (e == nb) {
+            if (segs < e) sv[swz<T>(segs)] = (T)s;
+            s = A(0);
+            segs = e;
+            ++j;
+            nb = soff[j + 1];
+          }
+          s = fma((A)sv[swz<T>(e)], (A)sx[swz<T>(e)], s);
+        }
+        sv[swz<T>(segs)] = (T)s;
+      }
+      __syncthreads();
+      // Row fold: segment at the row start, then one per lane boundary inside.
+      for (int j = threadIdx.x; j < R; j += kThreads) {
+        const int a = soff[j], e = soff[j + 1];
+        A sum = A(0);
+        if (a < e) {
+          sum = (A)sv[swz<T>(a)];
+          for (int q = (a / SEG + 1) * SEG; q < e; q += SEG) sum += (A)sv[swz<T>(q)];
+        }
+        if constexpr (has_preload<Epi>::value) {
+          if (j == (int)threadIdx.x) epi.row_pre(b.x + j, sum, pre, acc);
+          else epi.row(b.x + j, sum, acc);
+        } else {
+          epi.row(b.x + j, sum, acc);
+        }
+      }
+    } else if (R == 1) {
       // one long light row: lane chains in A, cross-lane sums in FP64
       A s = A(0);
       for (int i = threadIdx.x; i < len; i += kThreads)

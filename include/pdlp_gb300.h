@@ -255,6 +255,14 @@ int pdlp_gpu_rescale(const lp_problem_t *prob, const pdhg_parameters_t *params,
 int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *col_ind,
                   const double *vals, const double *x, double *y, int tile);
 
+/* As pdlp_gpu_spmv, with tile 512, 1024 or 2048 and a kernel variant:
+ * 0 staged, 1 register path for short-row tiles (tile 1024 only), 2 the
+ * register path with column and value arrays placed off 16-byte boundaries
+ * (its scalar-load fallback). */
+int pdlp_gpu_spmv_variant(int rows, int cols, const int *row_ptr, const int *col_ind,
+                          const double *vals, const double *x, double *y, int tile,
+                          int variant);
+
 /* Power method of the solver on the scaled problem of prob; returns the
  * step-size estimate sigma_max and the iteration count. */
 int pdlp_gpu_power_method(const lp_problem_t *prob,

@@ -21,13 +21,21 @@ def _csr_with_shapes(rng, rows, cols, lengths):
     return ptr, col, val
 
 
-@pytest.mark.parametrize("tile", [512, 2048])
-@pytest.mark.parametrize("shape", ["short", "mixed", "long", "empty_rows", "single"])
-def test_spmv_matches_oracle(lib, oracle, tile, shape):
+# (tile, kernel variant): staged tiles of 512, 1024 and 2048 non-zeros; the
+# register path for short-row tiles (1024), also on column and value arrays
+# off 16-byte boundaries (scalar loads)
+KERNELS = [(512, 0), (2048, 0), (1024, 0), (1024, 1), (1024, 2)]
+
+
+@pytest.mark.parametrize("tile,variant", KERNELS)
+@pytest.mark.parametrize("shape", ["short", "mixed", "long", "empty_rows", "single", "rows20"])
+def test_spmv_matches_oracle(lib, oracle, tile, variant, shape):
     rng = np.random.default_rng(11)
     cols = 60000
     if shape == "short":
         lengths = rng.integers(0, 12, size=3000)
+    elif shape == "rows20":  # rows of ~20 non-zeros: every tile on the register path
+        lengths = rng.poisson(20, size=4000)
     elif shape == "mixed":  # power-law rows: most light, some longer than a tile
         lengths = np.minimum(cols, (rng.pareto(1.1, size=2500) * 3).astype(int) + 1)
     elif shape == "long":
@@ -39,8 +47,8 @@ def test_spmv_matches_oracle(lib, oracle, tile, shape):
     ptr, col, val = _csr_with_shapes(rng, len(lengths), cols, lengths)
     x = rng.standard_normal(cols)
     y = np.zeros(len(lengths))
-    rc = lib.pdlp_gpu_spmv(len(lengths), cols, cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val),
-                           cp.as_dp(x), cp.as_dp(y), tile)
+    rc = lib.pdlp_gpu_spmv_variant(len(lengths), cols, cp.as_ip(ptr), cp.as_ip(col),
+                                   cp.as_dp(val), cp.as_dp(x), cp.as_dp(y), tile, variant)
     assert rc == 0
     yo = np.zeros(len(lengths))
     oracle.oracle_spmv(len(lengths), cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val), cp.as_dp(x),
@@ -52,9 +60,35 @@ def test_spmv_matches_oracle(lib, oracle, tile, shape):
     assert np.all(np.abs(y - yo) <= tol)
     # bitwise reproducible run to run
     y2 = np.zeros_like(y)
-    lib.pdlp_gpu_spmv(len(lengths), cols, cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val),
-                      cp.as_dp(x), cp.as_dp(y2), tile)
+    lib.pdlp_gpu_spmv_variant(len(lengths), cols, cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val),
+                              cp.as_dp(x), cp.as_dp(y2), tile, variant)
     assert np.array_equal(y, y2)
+
+
+def test_spmv_register_path_matches_staged_bitwise_on_aligned_and_offset_arrays(lib):
+    # the vector-load and scalar-load forms of the register path sum in the
+    # same order
+    rng = np.random.default_rng(5)
+    lengths = rng.poisson(20, size=3000)
+    ptr, col, val = _csr_with_shapes(rng, len(lengths), 50000, lengths)
+    x = rng.standard_normal(50000)
+    ys = []
+    for variant in (1, 2):
+        y = np.zeros(len(lengths))
+        assert lib.pdlp_gpu_spmv_variant(len(lengths), 50000, cp.as_ip(ptr), cp.as_ip(col),
+                                         cp.as_dp(val), cp.as_dp(x), cp.as_dp(y), 1024,
+                                         variant) == 0
+        ys.append(y)
+    assert np.array_equal(ys[0], ys[1])
+
+
+def test_spmv_variant_rejects_register_path_off_tile_1024(lib):
+    ptr = np.array([0, 1], dtype=np.int32)
+    col = np.array([0], dtype=np.int32)
+    val, x, y = np.ones(1), np.ones(1), np.zeros(1)
+    for tile, variant in ((512, 1), (2048, 2), (1024, 3), (1000, 0)):
+        assert lib.pdlp_gpu_spmv_variant(1, 1, cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val),
+                                         cp.as_dp(x), cp.as_dp(y), tile, variant) != 0
 
 
 def test_spmv_rejects_bad_columns(lib):
