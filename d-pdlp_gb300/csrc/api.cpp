@@ -389,7 +389,7 @@ bool prepare_params(const pdhg_parameters_t *params, pdhg_parameters_t &p) {
   if (p.presolve)
     std::call_once(g_presolve_notice, [] {
       fprintf(stderr,
-              "[cupdlpx-gb300] presolve requested: this build has no presolver; "
+              "[cupdlpx-gb300] presolve requested: this library has no presolver; "
               "solving the original problem.\n");
     });
   return true;

@@ -92,7 +92,7 @@ void usage(const char *prog) {
           "  -f, --feasibility_polishing         polish primal and dual feasibility\n"
           "      --eps_feas_polish <tolerance>   polishing tolerance, default 1e-6\n"
           "      --opt_norm <l2|linf>            norm of the optimality criteria, default l2\n"
-          "      --no_presolve                   (presolve is not available in this build)\n"
+          "      --no_presolve                   (this library has no presolver)\n"
           "      --precision <fp64|fp32|fp32m>   iteration arithmetic, default fp64\n",
           prog, INT32_MAX);
 }

@@ -55,7 +55,7 @@ class LineSource {
       g_ = gzopen(path, "rb");
       return g_ != nullptr;
 #else
-      fprintf(stderr, "ERROR: %s: this build reads no gzip files\n", path);
+      fprintf(stderr, "ERROR: %s: compiled without zlib, gzip files cannot be read\n", path);
       return false;
 #endif
     }

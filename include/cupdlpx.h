@@ -10,7 +10,7 @@
  *    stream per solve, no process-global state;
  *  - cupdlpx_result_free also releases reduced_cost;
  *  - presolve=true prints a one-line notice and solves without presolve
- *    (the PSLP presolver the reference links is not part of this build).
+ *    (the PSLP presolver the reference links is not part of this library).
  */
 #ifndef CUPDLPX_GB300_H
 #define CUPDLPX_GB300_H

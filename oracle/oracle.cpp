@@ -1,6 +1,6 @@
 // oracle.cpp -- CPU FP64 restatement of the reference's single-GPU PDHG solve.
 //
-// TEST INFRASTRUCTURE ONLY: the correctness checker for the CUDA solver and
+// TEST INFRASTRUCTURE ONLY: the oracle of the CUDA solver's parity tests and
 // the timed CPU baseline.  Nothing in the product links or calls this file.
 //
 // It restates, in plain loops:

@@ -1,8 +1,8 @@
 /*
  * oracle.h -- CPU FP64 restatement of the reference's single-GPU PDHG solve.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the correctness checker for the
- * CUDA solver and the timed CPU baseline; the product never links, loads or
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle of the CUDA solver's
+ * parity tests and the timed CPU baseline; the product never links, loads or
  * calls it.  Each function cites the reference code (D-PDLP, path:line) that
  * it restates.
  */

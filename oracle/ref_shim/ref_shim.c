@@ -1,6 +1,6 @@
 /* Link stubs for building the reference's host-side code as a test oracle.
- * The GPU driver (optimize) is not built here: there is no GPU in the build
- * container and the reference sources are not present on the GPU machine. */
+ * The reference's GPU loop (optimize) is not built: the oracle uses only its
+ * host-side code (rescaling, converters, defaults, criteria, MPS reader). */
 #include <stddef.h>
 typedef struct cupdlpx_result_t_opaque cupdlpx_result_t;
 cupdlpx_result_t *optimize(const void *params, const void *prob) {
