@@ -4,6 +4,9 @@
 // solver_impl.cuh; this file holds the pieces defined once: the non-template
 // kernels, the host transpose, the device-resident problem, and
 // Solve<double, double>.
+#include <algorithm>
+#include <thread>
+
 #include "solver_impl.cuh"
 
 namespace pdlp {
@@ -82,22 +85,54 @@ __global__ void __launch_bounds__(kThreads) k_pm_resid_fin(PowDev d) {
   }
 }
 
+// A^T in CSR, entries of each column in row order (a stable counting sort).
+// Matrices of 4M+ non-zeros are transposed by up to 8 threads, each owning a
+// range of columns (balanced by non-zeros) and scanning every row in order,
+// so the result is the serial one, bit for bit.
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
-                    std::vector<int> &tp, std::vector<int> &tj,
-                    std::vector<double> &tx) {
-  int nnz = ap[m];
+                    std::vector<int> &tp, host_buf<int> &tj, host_buf<double> &tx) {
+  const int nnz = ap[m];
   tp.assign((size_t)n + 1, 0);
   tj.resize(nnz);
   tx.resize(nnz);
-  for (int k = 0; k < nnz; ++k) tp[aj[k] + 1]++;
-  for (int c = 0; c < n; ++c) tp[c + 1] += tp[c];
-  std::vector<int> next(tp.begin(), tp.end() - 1);
-  for (int r = 0; r < m; ++r)
-    for (int k = ap[r]; k < ap[r + 1]; ++k) {
-      int pos = next[aj[k]]++;
-      tj[pos] = r;
-      tx[pos] = ax[k];
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int T = nnz >= 4000000 && n > 0 ? (int)std::min(8u, hw ? hw : 1u) : 1;
+  auto run = [&](auto &&f) {
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t) th.emplace_back(f, t);
+    f(0);
+    for (auto &x : th) x.join();
+  };
+  // column counts: thread t owns columns [n t / T, n (t+1) / T)
+  run([&](int t) {
+    const int c0 = (int)((long)n * t / T), c1 = (int)((long)n * (t + 1) / T);
+    for (int k = 0; k < nnz; ++k) {
+      const int c = aj[k];
+      if (c >= c0 && c < c1) tp[c + 1]++;
     }
+  });
+  for (int c = 0; c < n; ++c) tp[c + 1] += tp[c];
+  // scatter: column ranges of about nnz / T entries each
+  std::vector<int> cut(T + 1, n);
+  cut[0] = 0;
+  for (int t = 1; t < T; ++t)
+    cut[t] = std::max(cut[t - 1], (int)(std::lower_bound(tp.begin(), tp.end(),
+                                                         (int)((long)nnz * t / T)) - tp.begin()));
+  cut[T] = n;
+  run([&](int t) {
+    const int c0 = std::min(cut[t], n), c1 = std::min(cut[t + 1], n);
+    if (c0 >= c1) return;
+    std::vector<int> next(tp.begin() + c0, tp.begin() + c1);
+    for (int r = 0; r < m; ++r)
+      for (int k = ap[r]; k < ap[r + 1]; ++k) {
+        const int c = aj[k];
+        if (c >= c0 && c < c1) {
+          const int pos = next[c - c0]++;
+          tj[pos] = r;
+          tx[pos] = ax[k];
+        }
+      }
+  });
 }
 
 // Non-zeros per thread-block tile.  PDLP_SPMV_TILE (512, 1024 or 2048)
@@ -153,8 +188,9 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   P->nnz = nnz;
   P->tile = pick_tile(nnz);
   P->c0 = prob->objective_constant;
-  std::vector<int> tp, tj;
-  std::vector<double> tx;
+  std::vector<int> tp;
+  host_buf<int> tj;
+  host_buf<double> tx;
   host_transpose(m, n, prob->constraint_matrix_row_pointers, prob->constraint_matrix_col_indices,
                  prob->constraint_matrix_values, tp, tj, tx);
   std::vector<int4> blkA, blkT;

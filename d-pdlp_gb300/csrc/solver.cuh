@@ -10,7 +10,9 @@
 #include <array>
 #include <map>
 #include <memory>
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -315,10 +317,27 @@ void gpu_rescale(const pdhg_parameters_t &p, DevCsr &A, DevCsr &AT, double *c,
                  double *part, cudaStream_t st, double fixed_cb = 0.0,
                  double fixed_ob = 0.0);
 
+// Host buffer whose elements are left uninitialised on resize (filled
+// right after, by several threads: no serial zero-fill first).
+template <class T>
+struct uninit_alloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = uninit_alloc<U>;
+  };
+  template <class U>
+  void construct(U *) noexcept {}
+  template <class U, class... Args>
+  void construct(U *p, Args &&...args) {
+    ::new ((void *)p) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using host_buf = std::vector<T, uninit_alloc<T>>;
+
 // Stable transpose of a host CSR (rows of A^T ordered by original row).
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,
-                    std::vector<int> &tp, std::vector<int> &tj,
-                    std::vector<double> &tx);
+                    std::vector<int> &tp, host_buf<int> &tj, host_buf<double> &tx);
 
 // Options of the mixed-precision solve (refine.cu).
 struct RefineOptions {
