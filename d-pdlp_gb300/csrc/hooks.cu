@@ -1,5 +1,7 @@
-// hooks.cu -- device-level entry points used by the parity tests
+// hooks.cu -- device-level and host entry points used by the parity tests
 // (declared in include/pdlp_gb300.h).
+#include <string.h>
+
 #include <string>
 #include <vector>
 
@@ -109,4 +111,24 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
                              const double *vals, const double *x, double *y, int tile) {
   if (tile != 512 && tile != 2048) return -1;
   return pdlp_gpu_spmv_variant(rows, cols, row_ptr, col_ind, vals, x, y, tile, 0);
+}
+
+extern "C" int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *col_ind,
+                                   const double *vals, int *t_row_ptr, int *t_col_ind,
+                                   double *t_vals) {
+  if (m < 0 || n < 0 || !row_ptr || !t_row_ptr) return -1;
+  const int nnz = row_ptr[m];
+  if (nnz < 0 || (nnz > 0 && (!col_ind || !vals || !t_col_ind || !t_vals))) return -1;
+  for (int k = 0; k < nnz; ++k)
+    if (col_ind[k] < 0 || col_ind[k] >= n) return -1;
+  std::vector<int> tp;
+  pdlp::host_buf<int> tj;
+  pdlp::host_buf<double> tx;
+  pdlp::host_transpose(m, n, row_ptr, col_ind, vals, tp, tj, tx);
+  memcpy(t_row_ptr, tp.data(), sizeof(int) * ((size_t)n + 1));
+  if (nnz) {
+    memcpy(t_col_ind, tj.data(), sizeof(int) * (size_t)nnz);
+    memcpy(t_vals, tx.data(), sizeof(double) * (size_t)nnz);
+  }
+  return 0;
 }

@@ -263,6 +263,13 @@ int pdlp_gpu_spmv_variant(int rows, int cols, const int *row_ptr, const int *col
                           const double *vals, const double *x, double *y, int tile,
                           int variant);
 
+/* The host transpose of the upload path: A (m x n CSR) to A^T (n x m CSR),
+ * entries of each column in row order.  Outputs: t_row_ptr n+1, t_col_ind
+ * and t_vals nnz.  Returns 0, or -1 on invalid sizes or a NULL pointer. */
+int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *col_ind,
+                        const double *vals, int *t_row_ptr, int *t_col_ind,
+                        double *t_vals);
+
 /* Power method of the solver on the scaled problem of prob; returns the
  * step-size estimate sigma_max and the iteration count. */
 int pdlp_gpu_power_method(const lp_problem_t *prob,
