@@ -13,6 +13,7 @@
 //
 // No counterpart in the reference, which solves one LP per call
 // (src/cupdlpx.c:174-198); each request here runs that solve.
+#include <string.h>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -62,6 +63,7 @@ struct Request {
   Clock::time_point submitted, admitted, finished;
   cupdlpx_result_t *result = nullptr;
   int worker = -1;
+  double upload_s = 0.0, device_s = 0.0;  // host upload call; solve on the stream
   bool done = false;
   std::string error;
 };
@@ -117,8 +119,13 @@ struct pdlp_server {
         err = "no CUDA stream for this worker";
       } else {
         try {
+          const auto tu = Clock::now();
           std::unique_ptr<pdlp::DevProblem> P(pdlp::upload_problem(r->prob, st));
-          res = pdlp::solve_uploaded(*P, params, opts, st, nullptr);
+          r->upload_s = since(tu, Clock::now());
+          pdlp_solve_info_t si;
+          memset(&si, 0, sizeof(si));
+          res = pdlp::solve_uploaded(*P, params, opts, st, &si);
+          r->device_s = si.device_seconds;
           cudaStreamSynchronize(st);
         } catch (const std::exception &e) {
           err = e.what();
@@ -240,6 +247,8 @@ cupdlpx_result_t *pdlp_server_wait(pdlp_server_t *s, long long id, pdlp_request_
     info->latency_seconds = since(r->submitted, r->finished);
     info->worker = r->worker;
     info->device_bytes = r->bytes;
+    info->upload_seconds = r->upload_s;
+    info->device_seconds = r->device_s;
   }
   if (!r->result) pdlp::record_error("pdlp_server_wait: solve failed: " + r->error);
   return r->result;

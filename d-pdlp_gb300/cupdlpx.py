@@ -188,7 +188,8 @@ PRECISION_FP64, PRECISION_FP32_REFINE, PRECISION_FP32_MATRIX = 0, 1, 2
 class RequestInfo(C.Structure):
     _fields_ = [("queued_seconds", C.c_double), ("solve_seconds", C.c_double),
                 ("latency_seconds", C.c_double), ("worker", C.c_int),
-                ("device_bytes", C.c_longlong)]
+                ("device_bytes", C.c_longlong), ("upload_seconds", C.c_double),
+                ("device_seconds", C.c_double)]
 
 
 class ServerStats(C.Structure):

@@ -143,6 +143,11 @@ typedef struct {
   double latency_seconds;   /* submit -> result */
   int worker;               /* worker thread that solved it */
   long long device_bytes;   /* footprint the admission charged */
+  double upload_seconds;    /* host time of the upload (checks, transpose,
+                               plans, copies enqueued) */
+  double device_seconds;    /* the solve on the worker's stream, from CUDA
+                               events (waits behind other requests' kernels
+                               included) */
 } pdlp_request_info_t;
 
 typedef struct {

@@ -27,7 +27,9 @@ STRUCTS = {"LpProblem": "lp_problem_t", "RestartParameters": "restart_parameters
            "PdhgParameters": "pdhg_parameters_t", "Result": "cupdlpx_result_t",
            "MatrixDesc": "matrix_desc_t"}
 # this library's own structures (include/pdlp_gb300.h)
-EXT_STRUCTS = {"SolveInfo": "pdlp_solve_info_t", "Options": "pdlp_options_t"}
+EXT_STRUCTS = {"SolveInfo": "pdlp_solve_info_t", "Options": "pdlp_options_t",
+               "RequestInfo": "pdlp_request_info_t", "ServerStats": "pdlp_server_stats_t",
+               "BatchInfo": "pdlp_batch_info_t"}
 
 
 def declared_functions():

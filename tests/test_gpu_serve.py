@@ -74,6 +74,9 @@ def test_server_staggered_arrivals_equal_alone():
         _same(a, b)
         assert info["latency_seconds"] >= info["solve_seconds"] > 0
         assert info["device_bytes"] > 0
+        # the solve's stream time and the host upload lie inside the request's solve time
+        assert 0 < info["device_seconds"] <= info["solve_seconds"] + 1e-3
+        assert 0 <= info["upload_seconds"] <= info["solve_seconds"]
 
 
 def test_memory_budget_serialises_admission():
