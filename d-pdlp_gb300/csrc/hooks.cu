@@ -132,3 +132,28 @@ extern "C" int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *
   }
   return 0;
 }
+
+extern "C" int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *blocks,
+                              int cap, int *nblk, int *nlong, int *direct) {
+  using namespace pdlp;
+  if (rows < 0 || !row_ptr || !nblk || !nlong || !direct) return -1;
+  if (tile != 512 && tile != 1024 && tile != 2048) return -1;
+  if (row_ptr[0] != 0) return -1;
+  for (int r = 0; r < rows; ++r)
+    if (row_ptr[r] > row_ptr[r + 1]) return -1;
+  if (chunk <= 0) chunk = tile * 8 < 8192 ? tile * 8 : 8192;
+  std::vector<int4> blk;
+  std::vector<int2> lr;
+  build_plan_host(rows, row_ptr, tile, blk, lr, chunk);
+  *nblk = (int)blk.size();
+  *nlong = (int)lr.size();
+  *direct = tile == 1024 && plan_direct(blk, row_ptr[rows]);
+  if (blocks)
+    for (int i = 0; i < (int)blk.size() && i < cap; ++i) {
+      blocks[4 * i] = blk[i].x;
+      blocks[4 * i + 1] = blk[i].y;
+      blocks[4 * i + 2] = blk[i].z;
+      blocks[4 * i + 3] = blk[i].w;
+    }
+  return 0;
+}

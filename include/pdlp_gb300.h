@@ -268,6 +268,16 @@ int pdlp_gpu_spmv_variant(int rows, int cols, const int *row_ptr, const int *col
                           const double *vals, const double *x, double *y, int tile,
                           int variant);
 
+/* The SpMV plan the solver builds for a CSR matrix of `rows` rows: tiles of
+ * `tile` non-zeros (512, 1024 or 2048), long rows in chunks of `chunk`
+ * (>= tile; 0: the solver's default).  Writes up to `cap` blocks as
+ * {first row, end row or -(long row id + 1), first non-zero, end non-zero}
+ * into `blocks` (may be NULL), and the block count, long-row count and the
+ * register-path choice (1 or 0, tiles of 1024 only).  Returns 0, or -1 on
+ * invalid arguments or a malformed row pointer. */
+int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *blocks,
+                   int cap, int *nblk, int *nlong, int *direct);
+
 /* The host transpose of the upload path: A (m x n CSR) to A^T (n x m CSR),
  * entries of each column in row order.  Outputs: t_row_ptr n+1, t_col_ind
  * and t_vals nnz.  Returns 0, or -1 on invalid sizes or a NULL pointer. */
