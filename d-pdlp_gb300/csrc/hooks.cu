@@ -116,9 +116,11 @@ extern "C" int pdlp_gpu_spmv(int rows, int cols, const int *row_ptr, const int *
 extern "C" int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *col_ind,
                                    const double *vals, int *t_row_ptr, int *t_col_ind,
                                    double *t_vals) {
-  if (m < 0 || n < 0 || !row_ptr || !t_row_ptr) return -1;
+  if (m < 0 || n < 0 || !row_ptr || !t_row_ptr || row_ptr[0] != 0) return -1;
+  for (int r = 0; r < m; ++r)
+    if (row_ptr[r] > row_ptr[r + 1]) return -1;
   const int nnz = row_ptr[m];
-  if (nnz < 0 || (nnz > 0 && (!col_ind || !vals || !t_col_ind || !t_vals))) return -1;
+  if (nnz > 0 && (!col_ind || !vals || !t_col_ind || !t_vals)) return -1;
   for (int k = 0; k < nnz; ++k)
     if (col_ind[k] < 0 || col_ind[k] >= n) return -1;
   std::vector<int> tp;

@@ -280,7 +280,8 @@ int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *block
 
 /* The host transpose of the upload path: A (m x n CSR) to A^T (n x m CSR),
  * entries of each column in row order.  Outputs: t_row_ptr n+1, t_col_ind
- * and t_vals nnz.  Returns 0, or -1 on invalid sizes or a NULL pointer. */
+ * and t_vals nnz.  Returns 0, or -1 on invalid sizes, a NULL pointer, a
+ * malformed row pointer or a column index outside [0, n). */
 int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *col_ind,
                         const double *vals, int *t_row_ptr, int *t_col_ind,
                         double *t_vals);

@@ -41,3 +41,13 @@ def test_host_transpose_rejects_bad_columns(lib):
     tp, tj, tx = np.zeros(4, dtype=np.int32), np.zeros(2, dtype=np.int32), np.zeros(2)
     assert lib.pdlp_host_transpose(1, 3, cp.as_ip(ptr), cp.as_ip(col), cp.as_dp(val),
                                    cp.as_ip(tp), cp.as_ip(tj), cp.as_dp(tx)) == -1
+
+
+def test_host_transpose_rejects_malformed_row_pointers(lib):
+    col = np.array([0, 1], dtype=np.int32)
+    val = np.ones(2)
+    tp, tj, tx = np.zeros(3, dtype=np.int32), np.zeros(2, dtype=np.int32), np.zeros(2)
+    for ptr in ([0, 2, 1], [1, 1, 2]):  # decreasing; not starting at 0
+        p = np.array(ptr, dtype=np.int32)
+        assert lib.pdlp_host_transpose(2, 2, cp.as_ip(p), cp.as_ip(col), cp.as_dp(val),
+                                       cp.as_ip(tp), cp.as_ip(tj), cp.as_dp(tx)) == -1
