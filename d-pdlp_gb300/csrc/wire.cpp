@@ -92,7 +92,7 @@ lp_problem_t *pdlp_problem_deserialize(const void *buf, long long length) {
   if (n < 0 || m < 0 || nnz < 0) return nullptr;
   const unsigned char *c = r.take(8LL * n), *lv = r.take(8LL * n), *uv = r.take(8LL * n);
   const unsigned char *lc = r.take(8LL * m), *uc = r.take(8LL * m);
-  const unsigned char *rp = r.take(4LL * (m + 1)), *ci = r.take(4LL * nnz);
+  const unsigned char *rp = r.take(4LL * ((long long)m + 1)), *ci = r.take(4LL * nnz);
   const unsigned char *vx = r.take(8LL * nnz);
   int hp = 0, hd = 0;
   if (!c || !lv || !uv || !lc || !uc || !rp || !ci || !vx || !r.get(hp) || !r.get(hd))
@@ -114,7 +114,7 @@ lp_problem_t *pdlp_problem_deserialize(const void *buf, long long length) {
   double *cv = dvec(c, n), *lvv = dvec(lv, n), *uvv = dvec(uv, n), *lcv = dvec(lc, m),
          *ucv = dvec(uc, m), *vv = dvec(vx, nnz), *psv = hp ? dvec(ps, n) : nullptr,
          *dsv = hd ? dvec(ds, m) : nullptr;
-  int *rpv = ivec(rp, m + 1), *civ = ivec(ci, nnz);
+  int *rpv = ivec(rp, (long long)m + 1), *civ = ivec(ci, nnz);
   lp_problem_t *lp = nullptr;
   bool ok = cv && lvv && uvv && lcv && ucv && vv && rpv && civ && (!hp || psv) && (!hd || dsv);
   // the CSR must describe m rows and nnz entries in [0, n)

@@ -68,3 +68,24 @@ def test_rejects_truncated_and_inconsistent_payloads(lib):
     # a negative size
     with pytest.raises(ValueError):
         cp.Problem.from_bytes(struct.pack("<iiid", -1, 0, 0, 0.0) + b"\0" * 8, library=lib)
+
+
+def test_rejects_payloads_with_hostile_counts(lib):
+    # sizes near INT_MAX must be rejected by the length checks, never read
+    big = 2**31 - 1
+    for n, m, nnz in ((big, 0, 0), (0, big, 0), (0, 0, big), (big, big, big), (1, big, 1)):
+        head = struct.pack("<iiid", n, m, nnz, 0.0)
+        for tail in (b"", b"\0" * 64):
+            with pytest.raises(ValueError):
+                cp.Problem.from_bytes(head + tail, library=lib)
+    # random counts over a valid payload's bytes
+    prob = cp.Problem.generated("random", 20, 50, 120, 9, library=lib)
+    data = bytearray(prob.to_bytes())
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        bad = bytearray(data)
+        bad[:12] = struct.pack("<iii", *rng.integers(-5, 400, size=3))
+        try:
+            cp.Problem.from_bytes(bytes(bad), library=lib)
+        except ValueError:
+            pass
