@@ -72,7 +72,7 @@ long long pdlp_problem_serialize(const lp_problem_t *lp, void *buf, long long ca
   put(lp->variable_upper_bound, 8LL * n);
   put(lp->constraint_lower_bound, 8LL * m);
   put(lp->constraint_upper_bound, 8LL * m);
-  put(lp->constraint_matrix_row_pointers, 4LL * (m + 1));
+  put(lp->constraint_matrix_row_pointers, 4LL * ((long long)m + 1));
   put(lp->constraint_matrix_col_indices, 4LL * nnz);
   put(lp->constraint_matrix_values, 8LL * nnz);
   const int hp = lp->primal_start != nullptr, hd = lp->dual_start != nullptr;
