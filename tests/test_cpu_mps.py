@@ -92,3 +92,37 @@ def test_cli_usage_and_argument_errors():
     assert r.returncode == 1
     r = subprocess.run([cli, "--opt_norm", "l3", "a.mps", "out"], capture_output=True, text=True)
     assert r.returncode == 1
+
+
+def test_mutated_mps_files_parse_or_fail_cleanly(lib, tmp_path):
+    """Lines deleted, duplicated, truncated or replaced with noise: the reader
+    returns a problem or NULL, never crashes, and what it returns is a valid
+    CSR problem."""
+    import random
+    texts = [open(os.path.join(MPS_DIR, f)).read() for f in sorted(os.listdir(MPS_DIR))
+             if f.endswith(".mps")]
+    rng = random.Random(7)
+    path = tmp_path / "m.mps"
+    for _ in range(400):
+        lines = rng.choice(texts).split("\n")
+        for _ in range(rng.randint(1, 5)):
+            i = rng.randrange(len(lines))
+            op = rng.randint(0, 4)
+            if op == 0 and len(lines) > 1:
+                del lines[i]
+            elif op == 1:
+                lines.insert(i, rng.choice(lines))
+            elif op == 2:
+                lines[i] = lines[i][: rng.randrange(len(lines[i]) + 1)]
+            elif op == 3:
+                lines[i] += " " + rng.choice(["1e400", "-inf", "nan", "X", "9" * 30, "MARKER"])
+            else:
+                lines[i] = "".join(rng.choice("AB 01.-+eE\t") for _ in range(rng.randint(0, 30)))
+        path.write_text("\n".join(lines))
+        p = lib.read_mps_file(os.fsencode(str(path)))
+        if p:
+            a = cp.problem_arrays(p)
+            rp = a["row_ptr"]
+            assert rp[0] == 0 and np.all(np.diff(rp) >= 0) and rp[-1] == a["nnz"]
+            assert np.all((a["col_ind"] >= 0) & (a["col_ind"] < a["n"]))
+            lib.lp_problem_free(p)
