@@ -84,6 +84,10 @@ int csc_to_csr(const matrix_desc_t *d, int **rp, int **ci, double **v, int *nnz_
   const int *cp = d->data.csc.col_ptr, *ri = d->data.csc.row_ind;
   const double *x = d->data.csc.vals;
   const double tol = d->zero_tolerance > 0 ? d->zero_tolerance : 0.0;
+  // the column pointer must describe n columns over the declared non-zeros
+  if (!cp || cp[0] != 0 || cp[n] != d->data.csc.nnz) return -1;
+  for (int j = 0; j < n; ++j)
+    if (cp[j] > cp[j + 1]) return -1;
   std::vector<int> cnt((size_t)m + 1, 0);
   int nnz = 0;
   for (int j = 0; j < n; ++j)

@@ -163,3 +163,29 @@ def test_generators_are_deterministic(lib):
         for r in range(a["m"]):
             row = cj[rp[r]:rp[r + 1]]
             assert np.all(np.diff(row) > 0)
+
+
+def test_create_rejects_malformed_csc_and_coo(lib):
+    """CSC and COO inputs are converted on the host; a column pointer that is
+    not monotone or disagrees with the declared non-zeros, and indices
+    outside the matrix, give NULL instead of reads or writes out of bounds."""
+    c = np.zeros(3)
+    rows = np.array([0, 1, 1], dtype=np.int32)
+    cols = np.array([0, 2, 1], dtype=np.int32)
+    vals = np.ones(3)
+    for col_ptr, nnz in (([0, 2, 1, 3], 3), ([0, 1, 2, 3], 2), ([1, 1, 2, 3], 3)):
+        ptr = np.array(col_ptr, dtype=np.int32)
+        d = cp.MatrixDesc()
+        d.m, d.n, d.fmt, d.zero_tolerance = 2, 3, cp.MATRIX_CSC, 0.0
+        d.data.csc.nnz = nnz
+        d.data.csc.col_ptr, d.data.csc.row_ind, d.data.csc.vals = (
+            cp.as_ip(ptr), cp.as_ip(rows), cp.as_dp(vals))
+        assert not lib.create_lp_problem(cp.as_dp(c), C.byref(d), None, None, None, None, None)
+    for r, k in (([0, 2, 1], [0, 1, 2]), ([0, 1, 1], [0, 3, 1]), ([-1, 0, 1], [0, 1, 2])):
+        rr, kk = np.array(r, dtype=np.int32), np.array(k, dtype=np.int32)
+        d = cp.MatrixDesc()
+        d.m, d.n, d.fmt, d.zero_tolerance = 2, 3, cp.MATRIX_COO, 0.0
+        d.data.coo.nnz = 3
+        d.data.coo.row_ind, d.data.coo.col_ind, d.data.coo.vals = (
+            cp.as_ip(rr), cp.as_ip(kk), cp.as_dp(vals))
+        assert not lib.create_lp_problem(cp.as_dp(c), C.byref(d), None, None, None, None, None)
