@@ -177,7 +177,8 @@ struct pre_of<E, true> {
 // to 1024 non-zeros.  2048-element tiles need their registers (the long-row
 // path keeps 8 loads per thread in flight) and run at 4 blocks.  The
 // register-path variant holds a group's columns and values across the first
-// barrier and runs at 5 blocks (48 registers, no spills).
+// barrier and runs at 5 blocks (48 registers; no spills in the dual-step
+// instantiation, 16 bytes in the primal-step one).
 template <int TILE, bool DIRECT = false>
 constexpr int spmv_min_blocks() {
   return TILE >= 2048 ? 1 : DIRECT ? 5 : 6;
