@@ -685,9 +685,10 @@ pdlp_device_problem_t *pdlp_device_problem_create(const lp_problem_t *prob) {
   }
   try {
     StreamGuard sg;
-    auto *dp = new pdlp_device_problem;
+    auto dp = std::make_unique<pdlp_device_problem>();
     dp->P.reset(pdlp::upload_problem(prob, sg.s));
-    return dp;
+    dp->P->owner = cudaStreamPerThread;  // sg.s ends here; the upload has finished
+    return dp.release();
   } catch (const std::exception &e) {
     set_error(std::string("pdlp_device_problem_create: ") + e.what());
     cudaGetLastError();

@@ -74,6 +74,20 @@ double Rng::normal() {  // Marsaglia polar method, one draw per call
   }
 }
 
+// Frees a problem made by alloc_problem (the arrays and the struct, as
+// lp_problem_free does), so this file needs nothing else of the library.
+void free_problem(lp_problem_t *p) {
+  free(p->constraint_matrix_row_pointers);
+  free(p->constraint_matrix_col_indices);
+  free(p->constraint_matrix_values);
+  free(p->objective_vector);
+  free(p->variable_lower_bound);
+  free(p->variable_upper_bound);
+  free(p->constraint_lower_bound);
+  free(p->constraint_upper_bound);
+  free(p);
+}
+
 lp_problem_t *alloc_problem(int m, int n, long nnz) {
   lp_problem_t *p = (lp_problem_t *)calloc(1, sizeof(lp_problem_t));
   if (!p) return nullptr;
@@ -91,7 +105,7 @@ lp_problem_t *alloc_problem(int m, int n, long nnz) {
   if (!p->constraint_matrix_row_pointers || !p->constraint_matrix_col_indices ||
       !p->constraint_matrix_values || !p->objective_vector || !p->variable_lower_bound ||
       !p->variable_upper_bound || !p->constraint_lower_bound || !p->constraint_upper_bound) {
-    lp_problem_free(p);
+    free_problem(p);
     return nullptr;
   }
   return p;

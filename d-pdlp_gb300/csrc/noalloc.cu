@@ -125,11 +125,12 @@ __global__ void k_spmv_tiles_fix(int ntiles, const int *__restrict__ ptr, double
   y[r] = tot;
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, per device.  Only a successful
+// lookup is kept: a lookup that failed (say, before the device could be
+// used) is tried again by the next call.
 constexpr int kMaxDevices = 64;
 Scratch *g_addr[kMaxDevices] = {};
-std::once_flag g_once[kMaxDevices];
-cudaError_t g_setup_err[kMaxDevices] = {};
+std::mutex g_addr_mu;
 
 thread_local std::string g_err;
 
@@ -153,7 +154,10 @@ extern "C" int pdlp_spmv_noalloc(int rows, int cols, int nnz, const int *row_ptr
     return fail(-3, "nnz " + std::to_string(nnz) + " exceeds the maximum of " +
                         std::to_string((long)kMaxTiles * kTile) +
                         " non-zeros (PDLP_NOALLOC_MAX_TILES tiles of 2048)");
-  if (rows == 0) return 0;
+  if (rows == 0) {
+    if (nnz > 0) return fail(-1, "non-zeros given for a matrix without rows");
+    return 0;
+  }
   if (!row_ptr || !y || (nnz > 0 && (!col_ind || !vals || !x)))
     return fail(-1, "NULL buffer");
   const int ntiles = (int)ntiles_l;
@@ -162,15 +166,20 @@ extern "C" int pdlp_spmv_noalloc(int rows, int cols, int nnz, const int *row_ptr
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(-2, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
   // set-up, once per device, with that device current
-  std::call_once(g_once[dev], [dev] {
-    void *p = nullptr;
-    g_setup_err[dev] = cudaGetSymbolAddress(&p, g_scratch);
-    if (g_setup_err[dev] == cudaSuccess) g_addr[dev] = (Scratch *)p;
-  });
-  if (g_setup_err[dev] != cudaSuccess || !g_addr[dev])
-    return fail(-2, std::string("cudaGetSymbolAddress failed: ") +
-                        cudaGetErrorString(g_setup_err[dev]));
-  Scratch *s = g_addr[dev];
+  Scratch *s = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_addr_mu);
+    if (!g_addr[dev]) {
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_scratch);
+      if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(-2, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+      }
+      g_addr[dev] = (Scratch *)p;
+    }
+    s = g_addr[dev];
+  }
   cudaStream_t st = (cudaStream_t)stream;
   // the error flag must start at zero; every other slot a call reads, the
   // same call writes first

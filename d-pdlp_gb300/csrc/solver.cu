@@ -161,8 +161,7 @@ static int pick_chunk(int tile) {
 }
 
 DevProblem::~DevProblem() {
-  // no work of any solve is in flight on the problem when it is freed
-  if (arena) dev_free(arena, cudaStreamPerThread);
+  if (arena) dev_free(arena, owner);
 }
 
 DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
@@ -183,6 +182,7 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
     if (!ok) throw std::runtime_error("invalid CSR matrix (row pointers or column indices)");
   }
   auto P = std::make_unique<DevProblem>();
+  P->owner = st;
   P->m = m;
   P->n = n;
   P->nnz = nnz;

@@ -147,6 +147,12 @@ struct DevProblem {
   double delta_p = 1.0, delta_d = 1.0;  // correction scalings (x - xbar) Delta_p, ...
   void *arena = nullptr;  // owned device memory (null for a view)
   size_t bytes = 0;
+  // Stream the arena is released on: the stream that uploaded it, so on an
+  // error path (uploads or solve kernels still queued there) the release is
+  // ordered after that work.  A handle that outlives its upload stream
+  // (pdlp_device_problem_t) switches to the per-thread stream: its solves
+  // return only after their work on the problem has finished.
+  cudaStream_t owner = cudaStreamPerThread;
   ~DevProblem();
 };
 

@@ -312,10 +312,13 @@ int pdlp_gpu_power_method(const lp_problem_t *prob,
  * (134,217,728); larger inputs return -3 without launching.  All calls share
  * the one scratch array per device, so calls that overlap on the GPU (other
  * streams, other host threads) race and must be serialised by the caller.
- * The first call on each device looks up the array's device address with
- * that device current; make that first call before any stream capture.
+ * The first successful call on each device looks up the array's device
+ * address with that device current.  Every call waits for its own product
+ * (it reads the error flag back and synchronises the stream), so it must not
+ * be called while that stream is being captured into a CUDA graph.
  *
- * Returns 0 on success; -1 bad arguments, -2 CUDA error, -3 size above the
+ * Returns 0 on success; -1 bad arguments (negative sizes, NULL buffers,
+ * non-zeros without rows), -2 CUDA error, -3 size above the
  * limit, -4 malformed CSR (row pointers or column indices, detected on the
  * device; y is then unspecified).  pdlp_spmv_noalloc_error() gives the
  * message of the calling thread's last failure. */

@@ -1123,4 +1123,19 @@ void oracle_session_free(oracle_session_t *ss) {
   delete ss;
 }
 
+void oracle_problem_free(lp_problem_t *p) {
+  if (!p) return;
+  free(p->constraint_matrix_row_pointers);
+  free(p->constraint_matrix_col_indices);
+  free(p->constraint_matrix_values);
+  free(p->objective_vector);
+  free(p->variable_lower_bound);
+  free(p->variable_upper_bound);
+  free(p->constraint_lower_bound);
+  free(p->constraint_upper_bound);
+  free(p->primal_start);
+  free(p->dual_start);
+  free(p);
+}
+
 }  // extern "C"

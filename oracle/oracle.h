@@ -111,6 +111,16 @@ int oracle_restart_decision(const restart_parameters_t *rp, int F, int total,
                             int inner, double fpe, double init_fpe,
                             double *last_fpe);
 
+/* The seeded LP generators of the benchmarks (d-pdlp_gb300/csrc/lpgen.cpp,
+ * compiled into this library under these names), so CPU baselines and the
+ * reference's own solve get their problems without loading the product
+ * library.  Problems are released with oracle_problem_free. */
+lp_problem_t *oracle_generate_random_lp(int m, int n, long long nnz, unsigned long long seed);
+lp_problem_t *oracle_generate_powerlaw_lp(int m, int n, long long nnz_target, double zipf_s,
+                                          int max_degree, unsigned long long seed);
+lp_problem_t *oracle_generate_transport_lp(int sources, int sinks, unsigned long long seed);
+void oracle_problem_free(lp_problem_t *p);
+
 #ifdef __cplusplus
 }
 #endif

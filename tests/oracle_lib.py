@@ -1,13 +1,17 @@
-"""ctypes access to the test oracle (oracle/liboracle.so) and, where it was
-built, to the reference's own host code (oracle/_ref/libref_host.so).
+"""ctypes access to the test oracle (oracle/liboracle.so) and, where they
+were built, to the reference's own host code (oracle/_ref/libref_host.so)
+and its own single-GPU solve (oracle/_ref/ref_solve).
 
-Test infrastructure only: used by tests/, never by the product.
+Test and benchmark infrastructure only: used by tests/, __graft_entry__.smoke()
+and bench.py's baseline arms, never by the product.
 """
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 import subprocess
+import tempfile
 
 import numpy as np
 
@@ -17,8 +21,25 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "liboracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libref_host.so")
+REF_SOLVE = os.path.join(ORACLE_DIR, "_ref", "ref_solve")
+# copy of the reference files its single-GPU solve is built from (git-ignored;
+# made by `make -C oracle stage` where the reference checkout exists)
+REF_STAGE = os.path.join(ROOT, "baseline", "_ref", "D-PDLP")
 _dp, _ip = cp._dp, cp._ip
 _O = None
+
+
+def reference_dir() -> str:
+    """The reference checkout: $PDLP_REFERENCE_DIR, else the reference_path
+    recorded in BASELINE.json at the repository root ("" when neither)."""
+    env = os.environ.get("PDLP_REFERENCE_DIR")
+    if env:
+        return env
+    try:
+        with open(os.path.join(ROOT, "BASELINE.json")) as f:
+            return json.load(f).get("reference_path", "") or ""
+    except (OSError, ValueError):
+        return ""
 
 
 def build_oracle() -> None:
@@ -50,8 +71,112 @@ def load():
                                   C.POINTER(_dp), _ip]
     O.oracle_print_frequency.restype = C.c_int
     O.oracle_print_frequency.argtypes = [C.c_int]
+    O.oracle_generate_random_lp.restype = P
+    O.oracle_generate_random_lp.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_ulonglong]
+    O.oracle_generate_powerlaw_lp.restype = P
+    O.oracle_generate_powerlaw_lp.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double,
+                                              C.c_int, C.c_ulonglong]
+    O.oracle_generate_transport_lp.restype = P
+    O.oracle_generate_transport_lp.argtypes = [C.c_int, C.c_int, C.c_ulonglong]
+    O.oracle_problem_free.restype = None
+    O.oracle_problem_free.argtypes = [P]
     _O = O
     return O
+
+
+class OracleProblem:
+    """A seeded LP made by the oracle library's copy of the generators (the
+    same problems, bit for bit, as the product's pdlp_generate_*_lp); it has
+    the `ptr` / `arrays()` interface of cupdlpx.Problem."""
+
+    def __init__(self, kind: str, *args):
+        O = load()
+        fn = {"random": O.oracle_generate_random_lp, "powerlaw": O.oracle_generate_powerlaw_lp,
+              "transport": O.oracle_generate_transport_lp}[kind]
+        self.ptr = fn(*args)
+        if not self.ptr:
+            raise ValueError(f"generator {kind}{args} failed")
+        self._O = O
+
+    def arrays(self) -> dict:
+        return cp.problem_arrays(self.ptr)
+
+    def free(self):
+        if self.ptr:
+            self._O.oracle_problem_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def write_lp_file(problem, path: str) -> None:
+    """The problem in ref_solve's input layout (oracle/ref_shim/ref_solve.c)."""
+    a = problem.arrays()
+    with open(path, "wb") as f:
+        f.write(b"PDLPLP1\0")
+        np.array([a["m"], a["n"], a["nnz"], 0], dtype="<i4").tofile(f)
+        np.array([a["c0"]], dtype="<f8").tofile(f)
+        for k in ("c", "lv", "uv", "lc", "uc"):
+            np.ascontiguousarray(a[k], dtype="<f8").tofile(f)
+        np.ascontiguousarray(a["row_ptr"], dtype="<i4").tofile(f)
+        np.ascontiguousarray(a["col_ind"], dtype="<i4").tofile(f)
+        np.ascontiguousarray(a["vals"], dtype="<f8").tofile(f)
+
+
+def build_ref_gpu() -> bool:
+    """Build the reference's single-GPU solve from the staged copy (staging it
+    first where the reference checkout exists); False when neither exists or
+    the build fails."""
+    ref = reference_dir()
+    if ref and os.path.isdir(os.path.join(ref, "src")):
+        r = subprocess.run(["make", "-s", "-C", ORACLE_DIR, "stage", f"REF_DIR={ref}"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            return False
+    if not os.path.isdir(os.path.join(REF_STAGE, "src")):
+        return False
+    r = subprocess.run(["make", "-s", "-j8", "-C", ORACLE_DIR, "refgpu"], capture_output=True,
+                       text=True)
+    return r.returncode == 0 and os.path.exists(REF_SOLVE)
+
+
+def ref_gpu_available() -> bool:
+    return os.path.exists(REF_SOLVE)
+
+
+def ref_gpu_solve(problem, eps: float = 1e-4, iter_limit: int = 0, time_limit: float = 0.0,
+                  timeout: float | None = None, lp_file: str | None = None) -> dict:
+    """One solve by the reference's own single-GPU FP64 code (cuSPARSE/cuBLAS),
+    in a fresh process (its power-method start comes from a process-global
+    generator).  Returns the result scalars, `wall_s` (the solve_lp_problem
+    call) and the x, y, rc vectors.  `lp_file` reuses an LP file already
+    written by write_lp_file."""
+    if not ref_gpu_available():
+        raise RuntimeError("the reference's single-GPU solve is not built")
+    with tempfile.TemporaryDirectory() as d:
+        lp = lp_file
+        if lp is None:
+            lp = os.path.join(d, "lp.bin")
+            write_lp_file(problem, lp)
+        out = os.path.join(d, "out.bin")
+        cmd = [REF_SOLVE, lp, out, "--eps", repr(eps)]
+        if iter_limit > 0:
+            cmd += ["--iter-limit", str(iter_limit)]
+        if time_limit > 0:
+            cmd += ["--time-limit", repr(time_limit)]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_solve failed ({r.returncode}): {r.stderr[-2000:]}")
+        line = [ln for ln in r.stdout.splitlines() if ln.startswith("REF_RESULT ")][-1]
+        res = json.loads(line[len("REF_RESULT "):])
+        v = np.fromfile(out, dtype="<f8")
+        n, m = res["n"], res["m"]
+        res["x"], res["y"], res["rc"] = v[:n].copy(), v[n:n + m].copy(), v[n + m:].copy()
+        return res
 
 
 class RescaleInfo(C.Structure):

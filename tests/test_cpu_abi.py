@@ -16,10 +16,11 @@ import numpy as np
 import pytest
 
 import cupdlpx as cp
+import oracle_lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_INCLUDE = os.path.join(os.environ.get("PDLP_REFERENCE_DIR", "/root/reference"), "include")
+REF_INCLUDE = os.path.join(oracle_lib.reference_dir(), "include")
 SHIM = os.path.join(ROOT, "oracle", "ref_shim")
 
 STRUCTS = {"LpProblem": "lp_problem_t", "RestartParameters": "restart_parameters_t",
@@ -148,6 +149,8 @@ def test_noalloc_spmv_host_checks_need_no_gpu(lib):
     assert lib.pdlp_spmv_noalloc(1, 1, 65536 * 2048 + 1, None, None, None, None, None, None) == -3
     assert lib.pdlp_spmv_noalloc(-1, 1, 1, None, None, None, None, None, None) == -1
     assert lib.pdlp_spmv_noalloc(0, 5, 0, None, None, None, None, None, None) == 0
+    # non-zeros without rows is an inconsistent CSR, rejected before any CUDA call
+    assert lib.pdlp_spmv_noalloc(0, 5, 3, None, None, None, None, None, None) == -1
 
 
 def test_generators_are_deterministic(lib):
