@@ -39,6 +39,9 @@ def nvcc() -> str:
 def _flags(src: str) -> list[str]:
     f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC] + ARCH
+    # extra nvcc flags for tuning builds (e.g. -DPDLP_PIPE_CTAS=3); objects
+    # are rebuilt when they change
+    f += os.environ.get("PDLP_NVCC_FLAGS", "").split()
     if src == "lpgen.cpp":
         f += ["-Xcompiler", "-ffp-contract=off"]  # bit-identical on x86 and Arm
     if src.endswith(".cu") or src in ("api.cpp", "serve.cpp"):
@@ -59,12 +62,18 @@ def _headers_mtime() -> float:
 def _compile(src: str, hdr_time: float) -> str:
     out = os.path.join(OBJ, src + ".o")
     path = os.path.join(CSRC, src)
-    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(path), hdr_time):
+    stamp = out + ".flags"
+    flags = " ".join(_flags(src))
+    same_flags = os.path.exists(stamp) and open(stamp).read() == flags
+    if same_flags and os.path.exists(out) and \
+            os.path.getmtime(out) >= max(os.path.getmtime(path), hdr_time):
         return out
     cmd = [nvcc(), "-c", path, "-o", out] + _flags(src)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as fh:
+        fh.write(flags)
     return out
 
 

@@ -159,3 +159,33 @@ extern "C" int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk,
     }
   return 0;
 }
+
+extern "C" int pdlp_spmv_pipe_plan(int rows, const int *row_ptr, int nv, int *tiles, int *bytes,
+                                   int cap, int *ntile, int *nlong, int *limits) {
+  using namespace pdlp;
+  if (rows < 0 || !row_ptr || !ntile || !nlong || nv < 0) return -1;
+  if (row_ptr[0] != 0) return -1;
+  for (int r = 0; r < rows; ++r)
+    if (row_ptr[r] > row_ptr[r + 1]) return -1;
+  std::vector<int4> blk;
+  std::vector<int2> lr;
+  build_pipe_plan_host(rows, row_ptr, nv, blk, lr);
+  *ntile = (int)blk.size();
+  *nlong = (int)lr.size();
+  if (limits) {
+    limits[0] = kPipeRows;
+    limits[1] = kPipeTile;
+    limits[2] = kPipeMedRows;
+    limits[3] = kPipeStageBytes;
+  }
+  for (int i = 0; i < (int)blk.size() && i < cap; ++i) {
+    if (tiles) {
+      tiles[4 * i] = blk[i].x;
+      tiles[4 * i + 1] = blk[i].y;
+      tiles[4 * i + 2] = blk[i].z;
+      tiles[4 * i + 3] = blk[i].w;
+    }
+    if (bytes) bytes[i] = pipe_tile_bytes(blk[i], nv);
+  }
+  return 0;
+}

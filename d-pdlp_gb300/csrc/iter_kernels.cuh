@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include "solver.cuh"
+#include "spmv_pipe.cuh"
 
 namespace pdlp {
 
@@ -59,6 +60,17 @@ struct PrimalEpi {
   struct Pre {
     T xc, c, lv, uv, x0;
   };
+  // per-row vectors of the pipelined kernel, in Pre order
+  using vec_t = T;
+  static constexpr int NV = 5;
+  __device__ void vecs(const T *(&v)[NV]) const {
+    v[0] = xcur;
+    v[1] = d.c;
+    v[2] = d.lv;
+    v[3] = d.uv;
+    v[4] = d.x0;
+  }
+  __device__ Pre make_pre(const T (&v)[NV]) const { return Pre{v[0], v[1], v[2], v[3], v[4]}; }
   __device__ void preload(int j, Pre &p) const {
     p.xc = xcur[j];
     p.c = d.c[j];
@@ -121,6 +133,15 @@ struct DualEpi {
   struct Pre {
     T yc, lc, uc, y0;
   };
+  using vec_t = T;
+  static constexpr int NV = 4;
+  __device__ void vecs(const T *(&v)[NV]) const {
+    v[0] = ycur;
+    v[1] = d.lc;
+    v[2] = d.uc;
+    v[3] = d.y0;
+  }
+  __device__ Pre make_pre(const T (&v)[NV]) const { return Pre{v[0], v[1], v[2], v[3]}; }
   __device__ void preload(int i, Pre &p) const {
     p.yc = ycur[i];
     p.lc = d.lc[i];
@@ -349,9 +370,41 @@ __device__ __forceinline__ void set_steps(Ctl *c) {
   c->inv_sigma = 1.0 / c->sigma;
 }
 
+// Every SpMV of a solve runs the pipelined kernel when its matrix has a pipe
+// plan (and PDLP_STEP_KERNEL is not "fused"), else the fused kernel; the
+// sites' reduction partials follow the kernel that writes them.
+bool pipe_enabled();
+
+template <class V>
+inline bool use_pipe(const DevCsrT<V> &M) {
+  return M.pipe.ntile > 0 && pipe_enabled();
+}
+template <class V>
+inline size_t spmv_partials(const DevCsrT<V> &M) {
+  return use_pipe(M) ? (size_t)M.pipe.grid : (size_t)M.plan.nblk;
+}
+template <class V>
+inline size_t spmv_long_rows(const DevCsrT<V> &M) {
+  return use_pipe(M) ? (size_t)M.pipe.nlong : (size_t)M.plan.nlong;
+}
+
+template <class Epi>
+void set_pipe_smem() {
+  static const cudaError_t e = cudaFuncSetAttribute(
+      spmv_pipe<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+  PDLP_CUDA(e);
+}
+
 template <class Epi, class V>
 void launch_spmv(const DevCsrT<V> &M, const Epi &epi, double *part, double *lpart,
                  cudaStream_t st) {
+  if (use_pipe(M)) {
+    set_pipe_smem<Epi>();
+    spmv_pipe<Epi><<<M.pipe.grid, kThreads, kPipeSmem, st>>>(M.ptr, M.col, M.val, M.pipe, part,
+                                                               lpart, epi);
+    PDLP_LAUNCH_CHECK();
+    return;
+  }
   if (M.plan.nblk == 0) return;
   if (M.plan.tile == 2048)
     spmv_fused<2048, Epi><<<M.plan.nblk, kThreads, 0, st>>>(M.ptr, M.col, M.val, M.plan,

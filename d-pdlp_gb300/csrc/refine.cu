@@ -133,8 +133,10 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   auto need = [&](size_t b) { bytes += a256(b + 1); };
   for (int i = 0; i < 9; ++i) need(vn * 8);  // xbar lam z lz c2 lv2 uv2 rc xold
   for (int i = 0; i < 7; ++i) need(vm * 8);  // ybar w lc2 uc2 lcf ucf yold
-  need((size_t)P.A.plan.nlong * 4); need((size_t)P.A.plan.nblk * 8);
-  need((size_t)P.AT.plan.nlong * 4); need((size_t)P.AT.plan.nblk * 8);
+  for (const DevCsr *W : {&P.A, &P.AT}) {
+    need((size_t)W->plan.nlong * 4); need((size_t)W->plan.nblk * 8);
+    need((size_t)W->pipe.nlong * 4); need((size_t)W->pipe.ntile * 8); need(4);
+  }
   char *mem = (char *)dev_alloc(bytes, st);
   struct Free {
     char *p;
@@ -163,6 +165,14 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   AT.plan.lsum = (double *)take((size_t)P.AT.plan.nblk * 8);
   if (P.A.plan.nlong) PDLP_CUDA(cudaMemsetAsync(A.plan.lcnt, 0, (size_t)P.A.plan.nlong * 4, st));
   if (P.AT.plan.nlong) PDLP_CUDA(cudaMemsetAsync(AT.plan.lcnt, 0, (size_t)P.AT.plan.nlong * 4, st));
+  for (DevCsr *W : {&A, &AT}) {  // the pipelined kernel's scratch
+    W->pipe.lcnt = (unsigned *)take((size_t)W->pipe.nlong * 4);
+    W->pipe.lsum = (double *)take((size_t)W->pipe.ntile * 8);
+    W->pipe.err = (int *)take(4);
+    if (W->pipe.nlong)
+      PDLP_CUDA(cudaMemsetAsync(W->pipe.lcnt, 0, (size_t)W->pipe.nlong * 4, st));
+    PDLP_CUDA(cudaMemsetAsync(W->pipe.err, 0, sizeof(int), st));
+  }
   if (n) {
     PDLP_CUDA(cudaMemsetAsync(xbar, 0, vn * 8, st));
     PDLP_CUDA(cudaMemsetAsync(lam, 0, vn * 8, st));

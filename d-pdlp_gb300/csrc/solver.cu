@@ -4,6 +4,8 @@
 // solver_impl.cuh; this file holds the pieces defined once: the non-template
 // kernels, the host transpose, the device-resident problem, and
 // Solve<double, double>.
+#include <string.h>
+
 #include <algorithm>
 #include <thread>
 
@@ -160,6 +162,16 @@ static int pick_chunk(int tile) {
   return tile * 8 < 8192 ? tile * 8 : 8192;
 }
 
+// The SpMVs of a solve use the pipelined kernel when PDLP_STEP_KERNEL=pipe,
+// else the fused kernel.
+bool pipe_enabled() {
+  static const bool on = [] {
+    const char *e = getenv("PDLP_STEP_KERNEL");
+    return e && strcmp(e, "pipe") == 0;
+  }();
+  return on;
+}
+
 DevProblem::~DevProblem() {
   if (arena) dev_free(arena, owner);
 }
@@ -198,6 +210,15 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   const int chunk = pick_chunk(P->tile);
   build_plan_host(m, prob->constraint_matrix_row_pointers, P->tile, blkA, lrA, chunk);
   build_plan_host(n, tp.data(), P->tile, blkT, lrT, chunk);
+  // pipelined step kernel: the dual step (A) stages 4 row vectors, the
+  // primal step (A^T) 5
+  std::vector<int4> pblkA, pblkT;
+  std::vector<int2> plrA, plrT;
+  build_pipe_plan_host(m, prob->constraint_matrix_row_pointers, 4, pblkA, plrA);
+  build_pipe_plan_host(n, tp.data(), 5, pblkT, plrT);
+  int dev = 0, nsm = kNumSms;
+  PDLP_CUDA(cudaGetDevice(&dev));
+  PDLP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   // norms of the unscaled objective and bounds (reference pdlp_core_op.cu:232-286)
   {
     double ss = 0, mx = 0;
@@ -230,6 +251,8 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   z.add<int>(vn + 1); z.add<int>(nnz); z.add<double>(nnz);
   z.add<int4>(blkA.size()); z.add<int2>(lrA.size());
   z.add<int4>(blkT.size()); z.add<int2>(lrT.size());
+  z.add<int4>(pblkA.size()); z.add<int2>(plrA.size());
+  z.add<int4>(pblkT.size()); z.add<int2>(plrT.size());
   for (int i = 0; i < 3; ++i) z.add<double>(vn);
   for (int i = 0; i < 2; ++i) z.add<double>(vm);
   if (prob->primal_start) z.add<double>(vn);
@@ -237,7 +260,8 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   P->arena = dev_alloc(z.bytes, st);
   P->bytes = z.bytes;
   Arena ar{(char *)P->arena, 0};
-  auto mat = [&](DevCsr &M, int rows, int cols, std::vector<int4> &blk, std::vector<int2> &lr) {
+  auto mat = [&](DevCsr &M, int rows, int cols, std::vector<int4> &blk, std::vector<int2> &lr,
+                 std::vector<int4> &pblk, std::vector<int2> &plr) {
     M.rows = rows;
     M.cols = cols;
     M.nnz = nnz;
@@ -258,9 +282,19 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
       PDLP_CUDA(cudaMemcpyAsync(M.plan.blk, blk.data(), blk.size() * 16, cudaMemcpyHostToDevice, st));
     if (!lr.empty())
       PDLP_CUDA(cudaMemcpyAsync(M.plan.lrow, lr.data(), lr.size() * 8, cudaMemcpyHostToDevice, st));
+    M.pipe.ntile = (int)pblk.size();
+    M.pipe.nlong = (int)plr.size();
+    const long cap = (long)nsm * kPipeCtasPerSm;
+    M.pipe.grid = (int)(M.pipe.ntile < cap ? M.pipe.ntile : cap);
+    M.pipe.blk = ar.take<int4>(pblk.size());
+    M.pipe.lrow = ar.take<int2>(plr.size());
+    if (!pblk.empty())
+      PDLP_CUDA(cudaMemcpyAsync(M.pipe.blk, pblk.data(), pblk.size() * 16, cudaMemcpyHostToDevice, st));
+    if (!plr.empty())
+      PDLP_CUDA(cudaMemcpyAsync(M.pipe.lrow, plr.data(), plr.size() * 8, cudaMemcpyHostToDevice, st));
   };
-  mat(P->A, m, n, blkA, lrA);
-  mat(P->AT, n, m, blkT, lrT);
+  mat(P->A, m, n, blkA, lrA, pblkA, plrA);
+  mat(P->AT, n, m, blkT, lrT, pblkT, plrT);
   P->c = ar.take<double>(vn);
   P->lv = ar.take<double>(vn);
   P->uv = ar.take<double>(vn);

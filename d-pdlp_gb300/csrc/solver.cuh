@@ -18,16 +18,19 @@
 #include "common.cuh"
 #include "cupdlpx_types.h"
 #include "spmv.cuh"
+#include "spmv_pipe.cuh"
 
 namespace pdlp {
 
-// A sparse matrix resident in HBM (CSR, int32 indices, values of type T).
+// A sparse matrix resident in HBM (CSR, int32 indices, values of type T),
+// with the plans of the fused kernel and of the pipelined step kernel.
 template <class T>
 struct DevCsrT {
   int rows = 0, cols = 0, nnz = 0;
   int *ptr = nullptr, *col = nullptr;
   T *val = nullptr;
   SpmvPlan plan;
+  PipePlan pipe;
 };
 using DevCsr = DevCsrT<double>;
 
@@ -275,6 +278,7 @@ class Solve {
   int timed_iteration(int t0, int t1) const;
   void read_timing(int slot);
   void power_method();
+  void check_pipe_errors() const;
 
   pdhg_parameters_t p_;
   cudaStream_t st_;

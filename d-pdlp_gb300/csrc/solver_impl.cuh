@@ -461,12 +461,17 @@ void Solve<T, M>::alloc() {
   const int n = P_.n, m = P_.m, nnz = P_.nnz;
   const int ew = grid_for((long)n + m, 4);
   const size_t vn = n, vm = m;
-  const size_t nbA = P_.A.plan.nblk, nbT = P_.AT.plan.nblk;
-  const size_t nlA = P_.A.plan.nlong, nlT = P_.AT.plan.nlong;
+  // reduction partials of an SpMV site: one per CTA of the pipelined kernel
+  // (or per block of the fused kernel) plus one per long row
+  const size_t nbA = spmv_partials(P_.A), nbT = spmv_partials(P_.AT);
+  const size_t nlA = spmv_long_rows(P_.A), nlT = spmv_long_rows(P_.AT);
   Sizer z;
   z.add<double>(nnz); z.add<double>(nnz);                      // FP64 scaled values
   if (!M64) { z.add<M>(nnz); z.add<M>(nnz); }                  // iteration values
-  z.add<unsigned>(nlA); z.add<double>(nbA); z.add<unsigned>(nlT); z.add<double>(nbT);
+  for (const DevCsr *W : {&P_.A, &P_.AT}) {                    // SpMV scratch of both kernels
+    z.add<unsigned>(W->plan.nlong); z.add<double>(W->plan.nblk);
+    z.add<unsigned>(W->pipe.nlong); z.add<double>(W->pipe.ntile); z.add<int>(1);
+  }
   for (int i = 0; i < 3; ++i) z.add<double>(vn);               // c lv uv (FP64 scaled)
   for (int i = 0; i < 2; ++i) z.add<double>(vm);               // lc uc
   z.add<double>(vn); z.add<double>(vm);                        // Dc Dr
@@ -499,6 +504,11 @@ void Solve<T, M>::alloc() {
     W.plan.lcnt = ar.take<unsigned>(S.plan.nlong);
     W.plan.lsum = ar.take<double>(S.plan.nblk);
     if (S.plan.nlong) PDLP_CUDA(cudaMemsetAsync(W.plan.lcnt, 0, (size_t)S.plan.nlong * 4, st_));
+    W.pipe.lcnt = ar.take<unsigned>(S.pipe.nlong);
+    W.pipe.lsum = ar.take<double>(S.pipe.ntile);
+    W.pipe.err = ar.take<int>(1);
+    if (S.pipe.nlong) PDLP_CUDA(cudaMemsetAsync(W.pipe.lcnt, 0, (size_t)S.pipe.nlong * 4, st_));
+    PDLP_CUDA(cudaMemsetAsync(W.pipe.err, 0, sizeof(int), st_));
   };
   mat64(A64_, P_.A);
   mat64(AT64_, P_.AT);
@@ -509,6 +519,7 @@ void Solve<T, M>::alloc() {
     W.ptr = S64.ptr;
     W.col = S64.col;
     W.plan = S64.plan;  // shares the per-solve scratch of the FP64 copy
+    W.pipe = S64.pipe;
     if constexpr (M64) W.val = (M *)S64.val;
     else W.val = ar.take<M>(nnz);
   };
@@ -1013,6 +1024,20 @@ void Solve<T, M>::run() {
   }
   loop_sec_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   final_count_ = total_count();
+  check_pipe_errors();
+}
+
+// A stage wait of the pipelined kernel that timed out leaves a flag (the
+// kernel then stopped early, so the iterates are not to be trusted).
+template <class T, class M>
+void Solve<T, M>::check_pipe_errors() const {
+  int e[2] = {0, 0};
+  const int *flags[2] = {A64_.pipe.err, AT64_.pipe.err};
+  for (int i = 0; i < 2; ++i)
+    if (flags[i]) PDLP_CUDA(cudaMemcpyAsync(&e[i], flags[i], sizeof(int), cudaMemcpyDeviceToHost, st_));
+  PDLP_CUDA(cudaStreamSynchronize(st_));
+  if (e[0] || e[1])
+    throw std::runtime_error("pipelined SpMV: a tile copy did not complete within its wait limit");
 }
 
 // finite entries -> 0 (the dual feasibility problem's bounds)

@@ -278,6 +278,16 @@ int pdlp_gpu_spmv_variant(int rows, int cols, const int *row_ptr, const int *col
 int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *blocks,
                    int cap, int *nblk, int *nlong, int *direct);
 
+/* Tiling of the pipelined step kernel for a matrix of `rows` rows whose step
+ * epilogue stages nv per-row vectors: *ntile tiles of 4 ints {r0, r1 or
+ * -(long row id + 1), k0, k1} into tiles (up to cap) and, per tile, the stage
+ * bytes its copy ranges take in the largest precision into bytes (up to
+ * cap; either may be NULL); limits (may be NULL) receives {rows per tile,
+ * non-zeros per tile, longest row packed with others, stage bytes}.
+ * Returns 0, or -1 on invalid arguments or a malformed row pointer. */
+int pdlp_spmv_pipe_plan(int rows, const int *row_ptr, int nv, int *tiles, int *bytes,
+                        int cap, int *ntile, int *nlong, int *limits);
+
 /* The host transpose of the upload path: A (m x n CSR) to A^T (n x m CSR),
  * entries of each column in row order.  Outputs: t_row_ptr n+1, t_col_ind
  * and t_vals nnz.  Returns 0, or -1 on invalid sizes, a NULL pointer, a

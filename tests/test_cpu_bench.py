@@ -82,5 +82,7 @@ def test_reference_arm_prints_one_json_line(lib, oracle):
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "s" and d["higher_is_better"] is False
+    # without a GPU the FP64 oracle stands in for the reference's own GPU solve
     assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
+    assert d["config"]["workload"] == "random_m2k_n5k_nnz20k_seed0"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0

@@ -1,0 +1,105 @@
+"""Parity with the reference itself: the reference's own single-GPU FP64 solve
+(src/solver.cu optimize() through solve_lp_problem, cuSPARSE/cuBLAS, built
+from its sources by `make -C oracle refgpu`) against ours through the
+reference-compatible C API, on the configured seeded LPs.
+
+The bar is the stated one: same termination status, primal and dual
+objectives within 1e-6 relative, and our own KKT residuals at the requested
+tolerance.  Both codes run the same method in FP64 and differ only in
+summation order, so the iteration counts must agree closely and the result
+vectors (x, y and the reduced cost) stay close as well; those tolerances are
+set well above the differences measured on GB300 (counts equal; vectors
+within 2e-12 of max|v| at eps 1e-8) and far below anything a wrong
+step, projection or restart would give.
+
+Tests skip where the reference build is absent (no staged copy of its
+sources); the same checks against the CPU oracle run everywhere.
+"""
+import numpy as np
+import pytest
+
+import cupdlpx as cp
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+OBJ_TOL = 1e-6      # spec bar on the primal and dual objectives
+VEC_TOL = 1e-7      # max |a - b| / (1 + max |b|) on x, y, reduced cost
+
+
+def params(eps):
+    p = ol.oracle_params(ol.load())
+    p.termination_criteria.eps_optimal_relative = eps
+    p.termination_criteria.eps_feasible_relative = eps
+    return p
+
+
+def rel(a, b):
+    return abs(a - b) / (1.0 + abs(b))
+
+
+def vec_err(a, b):
+    return float(np.max(np.abs(a - b)) / (1.0 + np.max(np.abs(b)))) if len(b) else 0.0
+
+
+def assert_parity(ours, other, eps, iter_tol=0.02):
+    assert ours["status"] == other["status"] == "OPTIMAL"
+    for k in ("primal_objective_value", "dual_objective_value"):
+        assert rel(ours[k], other[k]) <= OBJ_TOL, (k, ours[k], other[k])
+    assert abs(ours["total_count"] - other["total_count"]) <= iter_tol * other["total_count"] + 10
+    for k in ("x", "y", "rc"):
+        assert vec_err(ours[k], other[k]) <= VEC_TOL, (k, vec_err(ours[k], other[k]))
+    # own KKT of the returned point meets the tolerance
+    assert ours["relative_primal_residual"] <= eps
+    assert ours["relative_dual_residual"] <= eps
+    assert ours["relative_objective_gap"] <= eps
+
+
+needs_ref = pytest.mark.skipif(not ol.ref_gpu_available(),
+                               reason="the reference's single-GPU solve is not built here")
+
+
+def cfg0():
+    # m = 2,000, n = 5,000, nnz = 20,000, uniform positions, seed 0
+    return cp.Problem.generated("random", 2000, 5000, 20000, 0)
+
+
+@pytest.mark.parametrize("eps", [1e-4, 1e-8])
+def test_cfg0_matches_cpu_oracle(eps):
+    prob = cfg0()
+    ours = cp.solve(prob, params(eps)).result
+    o, _ = ol.oracle_solve(ol.load(), prob, params(eps))
+    assert_parity(ours, o, eps)
+
+
+@needs_ref
+@pytest.mark.parametrize("eps", [1e-4, 1e-8])
+def test_cfg0_matches_reference_gpu_solve(eps):
+    prob = cfg0()
+    ours = cp.solve(prob, params(eps)).result
+    ref = ol.ref_gpu_solve(prob, eps=eps, timeout=600)
+    assert_parity(ours, ref, eps)
+
+
+@needs_ref
+def test_docs_example_matches_reference_gpu_solve():
+    # reference docs/C_API.md:47-90, optimum x = (1, 2), objective 3
+    prob = cp.Problem.from_csr([0, 2, 3, 5], [0, 1, 1, 0, 1], [1.0, 2.0, 1.0, 3.0, 2.0], 2,
+                               c=[1.0, 1.0], lc=[5.0, -np.inf, -np.inf], uc=[5.0, 2.0, 8.0])
+    ours = cp.solve(prob, params(1e-8)).result
+    ref = ol.ref_gpu_solve(prob, eps=1e-8, timeout=300)
+    assert ours["status"] == ref["status"] == "OPTIMAL"
+    assert abs(ours["total_count"] - ref["total_count"]) <= 20
+    for k in ("primal_objective_value", "dual_objective_value"):
+        assert rel(ours[k], ref[k]) <= OBJ_TOL
+    np.testing.assert_allclose(ours["x"], ref["x"], atol=1e-6)
+
+
+@needs_ref
+def test_transport_20m_matches_reference_gpu_solve():
+    # the configured transportation LP: 2,000 x 5,000 arcs (n = 10M, m =
+    # 7,000, nnz = 20M), eps 1e-4, both solves from the same seeded arrays
+    prob = cp.Problem.generated("transport", 2000, 5000, 2)
+    ours = cp.solve(prob, params(1e-4)).result
+    ref = ol.ref_gpu_solve(prob, eps=1e-4, timeout=900)
+    assert_parity(ours, ref, 1e-4)
