@@ -21,7 +21,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcupdlpx_gb300.so")
 
 SOURCES = ["solver.cu", "solver_f32.cu", "solver_mix.cu", "refine.cu", "precond.cu", "hooks.cu",
-           "noalloc.cu", "memory.cu",
+           "noalloc.cu", "memory.cu", "transpose.cu",
            "api.cpp", "serve.cpp", "lpgen.cpp", "mps.cpp", "wire.cpp"]
 CLI = os.path.join(HERE, "cupdlpx")
 # gzip-compressed MPS input where the zlib header and library exist

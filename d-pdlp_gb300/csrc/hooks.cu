@@ -1,5 +1,6 @@
 // hooks.cu -- device-level and host entry points used by the parity tests
 // (declared in include/pdlp_gb300.h).
+#include <stdio.h>
 #include <string.h>
 
 #include <string>
@@ -133,6 +134,56 @@ extern "C" int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *
     memcpy(t_vals, tx.data(), sizeof(double) * (size_t)nnz);
   }
   return 0;
+}
+
+extern "C" int pdlp_gpu_transpose(int m, int n, const int *row_ptr, const int *col_ind,
+                                  const double *vals, int *t_row_ptr, int *t_col_ind,
+                                  double *t_vals) {
+  if (m < 0 || n < 0 || !row_ptr || !t_row_ptr || row_ptr[0] != 0) return -1;
+  for (int r = 0; r < m; ++r)
+    if (row_ptr[r] > row_ptr[r + 1]) return -1;
+  const int nnz = row_ptr[m];
+  if (nnz > 0 && (!col_ind || !vals || !t_col_ind || !t_vals)) return -1;
+  for (int k = 0; k < nnz; ++k)
+    if (col_ind[k] < 0 || col_ind[k] >= n) return -1;
+  try {
+    using namespace pdlp;
+    const size_t nz = (size_t)nnz;
+    auto a256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t bytes = a256(((size_t)m + 1) * 4) + a256(nz * 4) + a256(nz * 8) +
+                         a256(((size_t)n + 1) * 4) + a256(nz * 4) + a256(nz * 8);
+    struct Free {
+      void *p = nullptr;
+      ~Free() {
+        if (p) cudaFree(p);
+      }
+    } mem, scr;
+    PDLP_CUDA(cudaMalloc(&mem.p, bytes));
+    PDLP_CUDA(cudaMalloc(&scr.p, device_transpose_scratch_bytes(n, nnz)));
+    char *p = (char *)mem.p;
+    int *dptr = (int *)p; p += a256(((size_t)m + 1) * 4);
+    int *dcol = (int *)p; p += a256(nz * 4);
+    double *dval = (double *)p; p += a256(nz * 8);
+    int *tptr = (int *)p; p += a256(((size_t)n + 1) * 4);
+    int *tcol = (int *)p; p += a256(nz * 4);
+    double *tval = (double *)p;
+    PDLP_CUDA(cudaMemcpy(dptr, row_ptr, ((size_t)m + 1) * 4, cudaMemcpyHostToDevice));
+    if (nnz) {
+      PDLP_CUDA(cudaMemcpy(dcol, col_ind, nz * 4, cudaMemcpyHostToDevice));
+      PDLP_CUDA(cudaMemcpy(dval, vals, nz * 8, cudaMemcpyHostToDevice));
+    }
+    device_transpose(m, n, nnz, dptr, dcol, dval, tptr, tcol, tval, scr.p, 0);
+    PDLP_CUDA(cudaMemcpy(t_row_ptr, tptr, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost));
+    if (nnz) {
+      PDLP_CUDA(cudaMemcpy(t_col_ind, tcol, nz * 4, cudaMemcpyDeviceToHost));
+      PDLP_CUDA(cudaMemcpy(t_vals, tval, nz * 8, cudaMemcpyDeviceToHost));
+    }
+    return 0;
+  } catch (const std::exception &e) {
+    fprintf(stderr, "[cupdlpx-gb300] pdlp_gpu_transpose: %s\n", e.what());
+    cudaGetLastError();
+    return -2;
+  }
 }
 
 extern "C" int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *blocks,

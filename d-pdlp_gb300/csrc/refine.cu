@@ -13,6 +13,7 @@
 // only has to represent the correction, which shrinks round after round.
 // Residuals, corrections and the final KKT are FP64 throughout.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
@@ -214,6 +215,19 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   Q.orig_ucf = oucf;
   Q.orig_c0 = P.c0;
 
+  // stall rule of the FP32 rounds: once a round's relative KKT error is
+  // below 2e-5 -- about where FP32 iterates (unit roundoff 6e-8) meet the
+  // cancellation of long rows -- the round ends when the error has not
+  // improved by 10% within max(10000, t / 2) iterations.  Above that level a
+  // plateau is the method's own (the 20M-nnz power-law LP, FP64 or FP32,
+  // spends 10,000+ iterations near 2e-4; FP32 alone reaches 1e-4 there in
+  // 57,000 iterations) and stopping there would hand an unconverged point to
+  // refinement.  PDLP_STALL_MIN / _FRAC / _FLOOR override the three numbers.
+  int stall_min = 10000;
+  double stall_frac = 0.5, stall_floor = 2e-5;
+  if (const char *e = getenv("PDLP_STALL_MIN")) stall_min = atoi(e);
+  if (const char *e = getenv("PDLP_STALL_FRAC")) stall_frac = atof(e);
+  if (const char *e = getenv("PDLP_STALL_FLOOR")) stall_floor = atof(e);
   RefineReport rep;
   double sigma = 0.0;
   int reason = TERMINATION_REASON_UNSPECIFIED;
@@ -275,7 +289,7 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
         rep.power_iterations = s.power_iterations();
         rep.sigma_max = sigma;
       }
-      s.set_stall_rule(10000, 0.5);  // a precision floor ends a round, never a hang
+      s.set_stall_rule(stall_min, stall_frac, stall_floor);  // a floor ends a round, never a hang
       s.enable_snapshot();
       s.run();
       if (round == 0) {

@@ -200,11 +200,14 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   P->nnz = nnz;
   P->tile = pick_tile(nnz);
   P->c0 = prob->objective_constant;
-  std::vector<int> tp;
-  host_buf<int> tj;
-  host_buf<double> tx;
-  host_transpose(m, n, prob->constraint_matrix_row_pointers, prob->constraint_matrix_col_indices,
-                 prob->constraint_matrix_values, tp, tj, tx);
+  // row pointers of A^T (column counts of A, prefix-summed) for the plans;
+  // A^T itself is built on the device after A is uploaded
+  std::vector<int> tp((size_t)n + 1, 0);
+  {
+    const int *cj = prob->constraint_matrix_col_indices;
+    for (int k = 0; k < nnz; ++k) tp[(size_t)cj[k] + 1]++;
+    for (int c = 0; c < n; ++c) tp[c + 1] += tp[c];
+  }
   std::vector<int4> blkA, blkT;
   std::vector<int2> lrA, lrT;
   const int chunk = pick_chunk(P->tile);
@@ -306,9 +309,14 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   h2d(P->A.ptr, prob->constraint_matrix_row_pointers, (vm + 1) * 4);
   h2d(P->A.col, prob->constraint_matrix_col_indices, (size_t)nnz * 4);
   h2d(P->A.val, prob->constraint_matrix_values, (size_t)nnz * 8);
-  h2d(P->AT.ptr, tp.data(), (vn + 1) * 4);
-  h2d(P->AT.col, tj.data(), (size_t)nnz * 4);
-  h2d(P->AT.val, tx.data(), (size_t)nnz * 8);
+  {
+    // stable transpose on the device (reference: cusparseCsr2cscEx2,
+    // src/pdlp_core_op.cu:109-130), scratch released on this stream
+    void *scratch = dev_alloc(device_transpose_scratch_bytes(n, nnz), st);
+    device_transpose(m, n, nnz, P->A.ptr, P->A.col, P->A.val, P->AT.ptr, P->AT.col, P->AT.val,
+                     scratch, st);
+    dev_free(scratch, st);
+  }
   h2d(P->c, prob->objective_vector, vn * 8);
   h2d(P->lv, prob->variable_lower_bound, vn * 8);
   h2d(P->uv, prob->variable_upper_bound, vn * 8);
@@ -322,7 +330,7 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
     P->ys = ar.take<double>(vm);
     h2d(P->ys, prob->dual_start, vm * 8);
   }
-  PDLP_CUDA(cudaStreamSynchronize(st));  // host staging (tp/tj/tx) must outlive the copies
+  PDLP_CUDA(cudaStreamSynchronize(st));  // host staging (plans) must outlive the copies
   return P.release();
 }
 

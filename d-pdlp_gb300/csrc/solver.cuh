@@ -56,11 +56,13 @@ struct Dev {
   int F, linf, verbose;
   double eps_opt, eps_feas, eps_inf, time_limit;
   double art, suff, nec, kp, ki, kd, ismooth;
-  // stall rule (FP32 rounds of the refinement): stop when the KKT error has
-  // not improved by 10% within max(stall_min, stall_frac * t) iterations;
-  // stall_min = 0 disables it
+  // stall rule (FP32 rounds of the refinement): once the KKT error is below
+  // stall_floor (near the resolution of FP32 iterates), stop when it has not
+  // improved by 10% within max(stall_min, stall_frac * t) iterations; above
+  // the floor a plateau is ordinary PDHG progress and the round goes on;
+  // stall_min = 0 disables the rule
   int stall_min;
-  double stall_frac;
+  double stall_frac, stall_floor;
   // shifted evaluation (refinement rounds): the solve works on a correction
   // LP centred at (sx, sy); the objectives are then those of the original
   // LP at (sx + x, sy + y), from its objective and finite bounds
@@ -186,9 +188,10 @@ class Solve {
     fixed_ob_ = ob;
   }
   // Enable the stall rule (before run()).
-  void set_stall_rule(int min_iters, double frac) {
+  void set_stall_rule(int min_iters, double frac, double floor) {
     d_.stall_min = min_iters;
     d_.stall_frac = frac;
+    d_.stall_floor = floor;
   }
   ~Solve();
   // Working copy of the problem, GPU rescaling, finite bounds, warm start.
@@ -344,6 +347,13 @@ struct uninit_alloc : std::allocator<T> {
 };
 template <class T>
 using host_buf = std::vector<T, uninit_alloc<T>>;
+
+// Stable transpose of a device CSR (rows of A^T ordered by original row),
+// bit for bit the host transpose below; scratch of
+// device_transpose_scratch_bytes(n, nnz) bytes, all work on stream st.
+size_t device_transpose_scratch_bytes(int n, int nnz);
+void device_transpose(int m, int n, int nnz, const int *ptr, const int *col, const double *val,
+                      int *tptr, int *tcol, double *tval, void *scratch, cudaStream_t st);
 
 // Stable transpose of a host CSR (rows of A^T ordered by original row).
 void host_transpose(int m, int n, const int *ap, const int *aj, const double *ax,

@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(kThreads)
       if (err < 0.9 * c->best_err) {
         c->best_err = err;
         c->best_err_t = t;
-      } else if (t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
+      } else if (c->best_err < d.stall_floor &&
+                 t - c->best_err_t > max(d.stall_min, (int)(d.stall_frac * t))) {
         stalled = true;
       }
     }

@@ -23,7 +23,8 @@
 // a row of more than kPipeMedRows non-zeros gets a tile of its own (one
 // block-wide sum); a row of more than kPipeTile non-zeros is cut into chunks
 // of kPipeTile, each summed by one tile, the last chunk to finish (atomic
-// ticket) adding the chunk sums in chunk order and running the epilogue.
+// ticket, checked by the CTA at its next tile) adding the chunk sums in
+// chunk order and running the epilogue.
 // Tile t runs on CTA t % grid, in increasing t: every sum has a fixed order,
 // so results are bitwise reproducible.
 //
@@ -52,19 +53,28 @@
 
 namespace pdlp {
 
-constexpr int kPipeRows = kThreads;      // rows per packed tile (one per thread)
-constexpr int kPipeTile = 2048;          // non-zeros per tile
-constexpr int kPipeMaxE = 9;             // elements per lane: odd, 256 x 9 >= kPipeTile
-constexpr int kPipeMedRows = 128;        // longer rows get a tile of their own
-constexpr int kPipeStageBytes = 25600;   // one stage buffer
-constexpr int kPipeStages = 2;           // tiles in flight per CTA
-// resident CTAs per SM: 4 x (2 x 25 KB + 1 KB) of 228 KB of shared memory,
-// 64 registers a thread (PDLP_PIPE_CTAS overrides it at build time)
-#ifdef PDLP_PIPE_CTAS
-constexpr int kPipeCtasPerSm = PDLP_PIPE_CTAS;
-#else
-constexpr int kPipeCtasPerSm = 4;
+// Shape of the pipeline (PDLP_PIPE_TILE / _STAGES / _CTAS override them at
+// build time): tiles of up to kPipeTile non-zeros in stage buffers of
+// kPipeStageBytes, kPipeStages stages a CTA (so kPipeStages - 1 tiles are in
+// flight while one is processed), kPipeCtasPerSm CTAs resident on an SM.
+#ifndef PDLP_PIPE_TILE
+#define PDLP_PIPE_TILE 2048
 #endif
+#ifndef PDLP_PIPE_STAGES
+#define PDLP_PIPE_STAGES 2
+#endif
+#ifndef PDLP_PIPE_CTAS
+#define PDLP_PIPE_CTAS 3
+#endif
+constexpr int kPipeRows = kThreads;      // rows per packed tile (one per thread)
+constexpr int kPipeTile = PDLP_PIPE_TILE;
+// elements per lane: the odd number at or above kPipeTile / 256
+constexpr int kPipeMaxE = ((kPipeTile + kThreads - 1) / kThreads) | 1;
+constexpr int kPipeMedRows = 128;        // longer rows get a tile of their own
+// a chunk of kPipeTile 8-byte values and their columns, plus copy padding
+constexpr int kPipeStageBytes = kPipeTile * 12 + 1024;
+constexpr int kPipeStages = PDLP_PIPE_STAGES;
+constexpr int kPipeCtasPerSm = PDLP_PIPE_CTAS;
 constexpr long long kPipeWaitCycles = 4000000000LL;  // ~2 s at 2 GHz, then give up
 
 // Byte layout of one tile in a stage buffer: row pointers [r0, r1], columns
@@ -173,14 +183,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+// L2 policy for data read once per sweep (the tile streams): evicted first,
+// so the gathered iterate vectors (8-80 MB) stay resident in the 129 MB L2
+// while ~0.5 GB of matrix streams through it every iteration.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
 // global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         uint64_t *bar) {
+                                         uint64_t *bar, uint64_t pol) {
   asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+      "[%0], [%1], %2, [%3], %4;" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
       : "memory");
+}
+// ticket of a long row's chunk: counts the arrival after this thread's
+// earlier writes (the chunk sum) are visible; returns the previous count
+__device__ __forceinline__ unsigned ticket_release(unsigned *p) {
+  unsigned prev;
+  asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(p) : "memory");
+  return prev;
 }
 
 // Bounded wait for a stage: false after kPipeWaitCycles without completion.
@@ -280,7 +305,6 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
   __shared__ __align__(8) uint64_t full[kPipeStages];
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
   __shared__ double sc[4];
-  __shared__ int s_last;
   __shared__ int s_fail;
 
   if (!epi.init()) return;
@@ -289,6 +313,7 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
   const int first = blockIdx.x;
   const int mine = first < plan.ntile ? (plan.ntile - 1 - first) / G + 1 : 0;
 
+  uint64_t pol = 0;
   auto issue = [&](int i) {  // tile i of this CTA into stage i % kPipeStages
     const T *vbase[NV > 0 ? NV : 1];
     if constexpr (NV > 0) epi.vecs(vbase);
@@ -299,14 +324,40 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
     uint64_t *bar = &full[i % kPipeStages];
     const int nvec = b.y >= 0 && L.b_vec > 0 ? NV : 0;
     mbar_arrive_expect_tx(bar, (unsigned)(L.b_ptr + L.b_col + L.b_val + nvec * L.b_vec));
-    if (L.b_ptr) bulk_g2s(st, ptr + L.a_ptr, L.b_ptr, bar);
-    if (L.b_col) bulk_g2s(st + L.o_col, col + L.a_col, L.b_col, bar);
-    if (L.b_val) bulk_g2s(st + L.o_val, val + L.a_val, L.b_val, bar);
+    if (L.b_ptr) bulk_g2s(st, ptr + L.a_ptr, L.b_ptr, bar, pol);
+    if (L.b_col) bulk_g2s(st + L.o_col, col + L.a_col, L.b_col, bar, pol);
+    if (L.b_val) bulk_g2s(st + L.o_val, val + L.a_val, L.b_val, bar, pol);
     for (int v = 0; v < nvec; ++v)
-      bulk_g2s(st + L.o_vec + v * L.b_vec, vbase[v] + L.a_vec, L.b_vec, bar);
+      bulk_g2s(st + L.o_vec + v * L.b_vec, vbase[v] + L.a_vec, L.b_vec, bar, pol);
+  };
+  // A long row's chunk counts its arrival without waiting for the count
+  // (thread 0 keeps the ticket); the check, and for the last chunk the
+  // row's sum and epilogue, run at the start of the CTA's next tile.
+  int pend_lid = -1, pend_row = 0;
+  unsigned pend_prev = 0;
+  int2 pend_lr = make_int2(0, 0);
+  auto finish_long = [&]() {
+    if (pend_lid < 0) return;
+    const int lid = pend_lid;
+    pend_lid = -1;
+    if (pend_prev != (unsigned)pend_lr.y - 1u) return;
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");  // every chunk sum is visible
+    double sum = 0.0;
+#pragma unroll 4
+    for (int c = 0; c < pend_lr.y; ++c) sum += __ldcg(plan.lsum + pend_lr.x + c);
+    double lacc[NF > 0 ? NF : 1];
+#pragma unroll
+    for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
+    epi.row(pend_row, (A)sum, lacc);
+    if constexpr (NF > 0) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
+    }
+    plan.lcnt[lid] = 0u;  // ready for the next launch
   };
 
   if (tid == 0) {
+    pol = l2_evict_first();
     for (int s = 0; s < kPipeStages; ++s) mbar_init(&full[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     epi.prologue(sc);
@@ -321,9 +372,12 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
   for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
 
   int i = 0;
+  int4 b_next = mine > 0 ? plan.blk[first] : make_int4(0, 0, 0, 0);
   for (; i < mine; ++i) {
     const int t = first + i * G;
-    const int4 b = plan.blk[t];
+    const int4 b = b_next;
+    if (i + 1 < mine) b_next = plan.blk[t + G];  // in flight while this tile runs
+    if (tid == 0) finish_long();
     const PipeLayout L = pipe_layout(b, (int)sizeof(M), (int)sizeof(T), NV);
     unsigned char *st = smem + (size_t)(i % kPipeStages) * kPipeStageBytes;
     if (!mbar_wait_bounded(&full[i % kPipeStages], (unsigned)((i / kPipeStages) & 1)))
@@ -368,24 +422,10 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
         } else {
           const int lid = -b.y - 1;
           plan.lsum[t] = tot;
-          __threadfence();
-          const unsigned prev = atomicAdd(plan.lcnt + lid, 1u);
-          s_last = (prev == (unsigned)plan.lrow[lid].y - 1u);
-          if (s_last) {
-            __threadfence();
-            const int2 LR = plan.lrow[lid];
-            double sum = 0.0;
-            for (int c = 0; c < LR.y; ++c) sum += __ldcg(plan.lsum + LR.x + c);
-            double lacc[NF > 0 ? NF : 1];
-#pragma unroll
-            for (int f = 0; f < (NF > 0 ? NF : 1); ++f) lacc[f] = 0.0;
-            epi.row(b.x, (A)sum, lacc);
-            if constexpr (NF > 0) {
-#pragma unroll
-              for (int f = 0; f < NF; ++f) lpart[f * plan.nlong + lid] = lacc[f];
-            }
-            plan.lcnt[lid] = 0u;  // ready for the next launch
-          }
+          pend_prev = ticket_release(plan.lcnt + lid);
+          pend_lr = plan.lrow[lid];  // both in flight until the next tile
+          pend_lid = lid;
+          pend_row = b.x;
         }
       }
     } else {
@@ -467,6 +507,7 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
       issue(i + kPipeStages);
     }
   }
+  if (tid == 0) finish_long();
   if (s_fail) {
     // a copy did not complete: report, wait (bounded) for the copies still
     // in flight into this CTA's stages, and leave
@@ -488,5 +529,10 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
 
 // Dynamic shared memory of the pipelined kernel.
 constexpr int kPipeSmem = kPipeStages * kPipeStageBytes;
+// kPipeCtasPerSm CTAs (each with ~2 KB of static shared memory and the 1 KB
+// the SM reserves per CTA) must fit the SM's 228 KB, or the grid would run
+// in two waves.
+static_assert(kPipeCtasPerSm * (kPipeSmem + 3 * 1024) <= 228 * 1024,
+              "pipeline stages do not fit kPipeCtasPerSm CTAs per SM");
 
 }  // namespace pdlp

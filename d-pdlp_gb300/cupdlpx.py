@@ -252,6 +252,8 @@ def _declare_ext(lib: C.CDLL) -> None:
                                           C.c_int]
     lib.pdlp_spmv_plan.restype = C.c_int
     lib.pdlp_spmv_plan.argtypes = [C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip]
+    lib.pdlp_gpu_transpose.restype = C.c_int
+    lib.pdlp_gpu_transpose.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp]
     lib.pdlp_spmv_pipe_plan.restype = C.c_int
     lib.pdlp_spmv_pipe_plan.argtypes = [C.c_int, _ip, C.c_int, _ip, _ip, C.c_int, _ip, _ip, _ip]
     lib.pdlp_host_transpose.restype = C.c_int

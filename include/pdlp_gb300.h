@@ -288,13 +288,21 @@ int pdlp_spmv_plan(int rows, const int *row_ptr, int tile, int chunk, int *block
 int pdlp_spmv_pipe_plan(int rows, const int *row_ptr, int nv, int *tiles, int *bytes,
                         int cap, int *ntile, int *nlong, int *limits);
 
-/* The host transpose of the upload path: A (m x n CSR) to A^T (n x m CSR),
+/* The host transpose (the order the device transpose reproduces): A (m x n CSR) to A^T (n x m CSR),
  * entries of each column in row order.  Outputs: t_row_ptr n+1, t_col_ind
  * and t_vals nnz.  Returns 0, or -1 on invalid sizes, a NULL pointer, a
  * malformed row pointer or a column index outside [0, n). */
 int pdlp_host_transpose(int m, int n, const int *row_ptr, const int *col_ind,
                         const double *vals, int *t_row_ptr, int *t_col_ind,
                         double *t_vals);
+
+/* The device transpose of the upload path (the stable transpose above,
+ * built on the GPU by a radix sort of the column indices), on host arrays
+ * copied in and out.  Returns 0, -1 as pdlp_host_transpose, -2 on a CUDA
+ * error. */
+int pdlp_gpu_transpose(int m, int n, const int *row_ptr, const int *col_ind,
+                       const double *vals, int *t_row_ptr, int *t_col_ind,
+                       double *t_vals);
 
 /* Power method of the solver on the scaled problem of prob; returns the
  * step-size estimate sigma_max and the iteration count. */

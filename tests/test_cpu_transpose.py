@@ -1,6 +1,7 @@
-"""The upload path's host transpose (pdlp_host_transpose) against SciPy's
-CSR -> CSC conversion, a stable counting sort: bit-identical outputs, below
-and above the size at which the transpose runs on several threads."""
+"""The host transpose (pdlp_host_transpose) -- the order the upload path's
+device transpose reproduces -- against SciPy's CSR -> CSC conversion, a
+stable counting sort: bit-identical outputs, below and above the size at
+which the transpose runs on several threads."""
 import numpy as np
 import pytest
 
