@@ -492,6 +492,23 @@ def run_batch(args, cp):
                    <= 10 * args.eps * (1 + abs(b["primal_objective_value"]))
                    for a, b in zip(res, seq))
     value = statistics.mean(vals)
+    # the reference's own single-GPU FP64 solve, LP after LP in batch order
+    # (a fresh process each), for about a minute: sequential LPs/s
+    ref_seq = None
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    if oracle_lib.ref_gpu_available() and gpu_visible():
+        t0, k = time.perf_counter(), 0
+        try:
+            while k < count and time.perf_counter() - t0 < args.ref_seconds:
+                oracle_lib.ref_gpu_solve(lps[k], eps=args.eps, timeout=600)
+                k += 1
+            el = time.perf_counter() - t0
+            ref_seq = {"lps_per_second": round(k / el, 3), "lps": k, "seconds": round(el, 2),
+                       "api": "the reference's solve_lp_problem (single-GPU FP64 build), one "
+                              "process per LP, the first LPs of the batch in order"}
+        except (RuntimeError, OSError) as e:
+            ref_seq = {"unavailable": str(e)[:200]}
     cpu = None
     if not args.no_cpu_baseline:
         # the FP64 oracle on every host core, LPs in batch order for ~15 s
@@ -523,6 +540,7 @@ def run_batch(args, cp):
                 "api": "pdlp_batch_solve from host arrays (upload, solve, copy-back per LP)"},
         "sequential": {"lps_per_second": round(count / t_seq, 2), "seconds": round(t_seq, 2),
                        "api": "solve_lp_problem, one LP after another"},
+        "reference_sequential": ref_seq,
         "batch": {"iterations": iters, "failed": failed, "max_concurrent": info["max_concurrent"],
                   "statuses": statuses, "worst_relative_kkt": worst,
                   "results_match_sequential": same},
@@ -718,6 +736,9 @@ def main():
     ap.add_argument("--duration", type=float, default=0.0,
                     help="serving workload: arrival window in seconds (0: the workload's 60)")
     ap.add_argument("--eps", type=float, default=1e-4)
+    ap.add_argument("--ref-seconds", type=float, default=60.0,
+                    help="batch workload: seconds of sequential solves by the reference's "
+                         "own GPU build")
     ap.add_argument("--kernel-reps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default=None,

@@ -227,7 +227,7 @@ extern "C" int pdlp_spmv_pipe_plan(int rows, const int *row_ptr, int nv, int *ti
     limits[0] = kPipeRows;
     limits[1] = kPipeTile;
     limits[2] = kPipeMedRows;
-    limits[3] = kPipeStageBytes;
+    limits[3] = kPipeTileBytes;
   }
   for (int i = 0; i < (int)blk.size() && i < cap; ++i) {
     if (tiles) {

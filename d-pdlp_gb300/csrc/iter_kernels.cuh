@@ -400,8 +400,8 @@ void launch_spmv(const DevCsrT<V> &M, const Epi &epi, double *part, double *lpar
                  cudaStream_t st) {
   if (use_pipe(M)) {
     set_pipe_smem<Epi>();
-    spmv_pipe<Epi><<<M.pipe.grid, kThreads, kPipeSmem, st>>>(M.ptr, M.col, M.val, M.pipe, part,
-                                                               lpart, epi);
+    spmv_pipe<Epi><<<M.pipe.grid, kPipeBlock, kPipeSmem, st>>>(M.ptr, M.col, M.val, M.pipe,
+                                                                 part, lpart, epi);
     PDLP_LAUNCH_CHECK();
     return;
   }

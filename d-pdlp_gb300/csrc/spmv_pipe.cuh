@@ -18,7 +18,7 @@
 // for the gather and the row outputs.
 //
 // Tiles (host plan, build_pipe_plan_host): consecutive rows [r0, r1) packed
-// while at most kPipeRows rows, kPipeTile non-zeros and kPipeStageBytes of
+// while at most kPipeRows rows, kPipeTile non-zeros and kPipeTileBytes of
 // stage buffer (all ranges, padded to their 16-byte copy boundaries) fit;
 // a row of more than kPipeMedRows non-zeros gets a tile of its own (one
 // block-wide sum); a row of more than kPipeTile non-zeros is cut into chunks
@@ -61,18 +61,24 @@ namespace pdlp {
 #define PDLP_PIPE_TILE 2048
 #endif
 #ifndef PDLP_PIPE_STAGES
-#define PDLP_PIPE_STAGES 2
+#define PDLP_PIPE_STAGES 3
 #endif
 #ifndef PDLP_PIPE_CTAS
-#define PDLP_PIPE_CTAS 3
+#define PDLP_PIPE_CTAS 2
 #endif
 constexpr int kPipeRows = kThreads;      // rows per packed tile (one per thread)
 constexpr int kPipeTile = PDLP_PIPE_TILE;
 // elements per lane: the odd number at or above kPipeTile / 256
 constexpr int kPipeMaxE = ((kPipeTile + kThreads - 1) / kThreads) | 1;
 constexpr int kPipeMedRows = 128;        // longer rows get a tile of their own
-// a chunk of kPipeTile 8-byte values and their columns, plus copy padding
-constexpr int kPipeStageBytes = kPipeTile * 12 + 1024;
+// a tile's copies: a chunk of kPipeTile 8-byte values and their columns,
+// plus copy padding; the stage adds room for the 256 lane sums of a one-row
+// tile (a double, or a float pair)
+constexpr int kPipeTileBytes = kPipeTile * 12 + 1024;
+constexpr int kPipeStageBytes = kPipeTileBytes + kThreads * 8;
+static_assert(kPipeStageBytes - kPipeTileBytes >= kThreads * 8 &&
+                  kPipeStageBytes - kPipeTileBytes >= kThreads * 2 * 4,
+              "lane-sum area of a stage");
 constexpr int kPipeStages = PDLP_PIPE_STAGES;
 constexpr int kPipeCtasPerSm = PDLP_PIPE_CTAS;
 constexpr long long kPipeWaitCycles = 4000000000LL;  // ~2 s at 2 GHz, then give up
@@ -151,7 +157,7 @@ inline void build_pipe_plan_host(int rows, const int *ptr, int NV, std::vector<i
       while (r < rows && r - r0 < kPipeRows) {
         const int l2 = ptr[r + 1] - ptr[r];
         if (l2 > kPipeMedRows || ptr[r + 1] - ptr[r0] > kPipeTile) break;
-        if (pipe_tile_bytes(make_int4(r0, r + 1, ptr[r0], ptr[r + 1]), NV) > kPipeStageBytes) break;
+        if (pipe_tile_bytes(make_int4(r0, r + 1, ptr[r0], ptr[r + 1]), NV) > kPipeTileBytes) break;
         ++r;
       }
     }
@@ -285,13 +291,36 @@ struct PipePlan {
   int *err = nullptr;         // per solve: set when a stage wait timed out
 };
 
+// Threads of the pipelined kernel: kThreads consumers (8 warps) and one
+// producer warp that issues the stage copies.
+constexpr int kPipeBlock = kThreads + 32;
+
+// The consumers' barrier (named barrier 1, kThreads threads): the producer
+// warp never waits on it.
+__device__ __forceinline__ void consumers_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Epi has the fused kernel's interface; the step epilogues also declare
 // `static constexpr int NV`, `vec_t`, `vecs(const vec_t *(&)[NV])` (the
 // per-row vectors, each read at the row index) and
 // `make_pre(const vec_t (&)[NV])` (the row's preloaded values), and then get
 // those vectors from the stage buffer.
+//
+// Roles: the producer warp's lane 0 issues tile i's copies into stage
+// i % kPipeStages once the consumers have released that stage (empty
+// mbarrier, one arrival per consumer warp); the 8 consumer warps wait for
+// the stage (full mbarrier, completed by the copies' byte count), process
+// the tile with one consumers-only barrier in the middle, and release it.
+// Every wait is bounded: a consumer whose stage never arrives marks itself
+// bad, skips the work that reads the stage but keeps to the barriers (so no
+// barrier waits on a thread that left), and the CTA reports the timeout in
+// plan.err.
 template <class Epi>
-__global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
+__global__ void __launch_bounds__(kPipeBlock, kPipeCtasPerSm)
     spmv_pipe(const int *__restrict__ ptr, const int *__restrict__ col,
               const typename Epi::val_t *__restrict__ val, PipePlan plan,
               double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
@@ -303,9 +332,9 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
   static_assert(sizeof(A) == sizeof(M), "run partials share the value buffer");
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[kPipeStages];
+  __shared__ __align__(8) uint64_t empty[kPipeStages];
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
   __shared__ double sc[4];
-  __shared__ int s_fail;
 
   if (!epi.init()) return;
   const int tid = threadIdx.x;
@@ -313,23 +342,50 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
   const int first = blockIdx.x;
   const int mine = first < plan.ntile ? (plan.ntile - 1 - first) / G + 1 : 0;
 
-  uint64_t pol = 0;
-  auto issue = [&](int i) {  // tile i of this CTA into stage i % kPipeStages
-    const T *vbase[NV > 0 ? NV : 1];
-    if constexpr (NV > 0) epi.vecs(vbase);
-    const int t = first + i * G;
-    const int4 b = plan.blk[t];
-    const PipeLayout L = pipe_layout(b, (int)sizeof(M), (int)sizeof(T), NV);
-    unsigned char *st = smem + (size_t)(i % kPipeStages) * kPipeStageBytes;
-    uint64_t *bar = &full[i % kPipeStages];
-    const int nvec = b.y >= 0 && L.b_vec > 0 ? NV : 0;
-    mbar_arrive_expect_tx(bar, (unsigned)(L.b_ptr + L.b_col + L.b_val + nvec * L.b_vec));
-    if (L.b_ptr) bulk_g2s(st, ptr + L.a_ptr, L.b_ptr, bar, pol);
-    if (L.b_col) bulk_g2s(st + L.o_col, col + L.a_col, L.b_col, bar, pol);
-    if (L.b_val) bulk_g2s(st + L.o_val, val + L.a_val, L.b_val, bar, pol);
-    for (int v = 0; v < nvec; ++v)
-      bulk_g2s(st + L.o_vec + v * L.b_vec, vbase[v] + L.a_vec, L.b_vec, bar, pol);
-  };
+  if (tid == 0) {
+    for (int q = 0; q < kPipeStages; ++q) {
+      mbar_init(&full[q], 1);
+      mbar_init(&empty[q], kThreads / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    epi.prologue(sc);
+  }
+  __syncthreads();
+  epi.bind(sc);
+
+  if (tid >= kThreads) {
+    // producer warp
+    if (tid == kThreads) {
+      const uint64_t pol = l2_evict_first();
+      const T *vbase[NV > 0 ? NV : 1];
+      if constexpr (NV > 0) epi.vecs(vbase);
+      for (int i = 0; i < mine; ++i) {
+        const int q = i % kPipeStages;
+        if (i >= kPipeStages &&
+            !mbar_wait_bounded(&empty[q], (unsigned)((i / kPipeStages - 1) & 1))) {
+          atomicOr(plan.err, 1);  // the consumers' waits then time out too
+          break;
+        }
+        const int4 b = plan.blk[first + i * G];
+        const PipeLayout L = pipe_layout(b, (int)sizeof(M), (int)sizeof(T), NV);
+        unsigned char *st = smem + (size_t)q * kPipeStageBytes;
+        uint64_t *bar = &full[q];
+        const int nvec = b.y >= 0 && L.b_vec > 0 ? NV : 0;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive_expect_tx(bar, (unsigned)(L.b_ptr + L.b_col + L.b_val + nvec * L.b_vec));
+        if (L.b_ptr) bulk_g2s(st, ptr + L.a_ptr, L.b_ptr, bar, pol);
+        if (L.b_col) bulk_g2s(st + L.o_col, col + L.a_col, L.b_col, bar, pol);
+        if (L.b_val) bulk_g2s(st + L.o_val, val + L.a_val, L.b_val, bar, pol);
+        for (int v = 0; v < nvec; ++v)
+          bulk_g2s(st + L.o_vec + v * L.b_vec, vbase[v] + L.a_vec, L.b_vec, bar, pol);
+      }
+    }
+    return;
+  }
+
+  // ---------------------------------------------------------- consumers
+  const int lane = tid & 31, warp = tid >> 5;
+  bool bad = false;
   // A long row's chunk counts its arrival without waiting for the count
   // (thread 0 keeps the ticket); the check, and for the last chunk the
   // row's sum and epilogue, run at the start of the CTA's next tile.
@@ -356,34 +412,23 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
     plan.lcnt[lid] = 0u;  // ready for the next launch
   };
 
-  if (tid == 0) {
-    pol = l2_evict_first();
-    for (int s = 0; s < kPipeStages; ++s) mbar_init(&full[s], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    epi.prologue(sc);
-    s_fail = 0;
-    for (int i = 0; i < kPipeStages && i < mine; ++i) issue(i);
-  }
-  __syncthreads();
-  epi.bind(sc);
-
   double acc[NF > 0 ? NF : 1];
 #pragma unroll
   for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
 
-  int i = 0;
   int4 b_next = mine > 0 ? plan.blk[first] : make_int4(0, 0, 0, 0);
-  for (; i < mine; ++i) {
+  for (int i = 0; i < mine; ++i) {
     const int t = first + i * G;
+    const int q = i % kPipeStages;
     const int4 b = b_next;
     if (i + 1 < mine) b_next = plan.blk[t + G];  // in flight while this tile runs
-    if (tid == 0) finish_long();
+    if (tid == 0 && !bad) finish_long();
     const PipeLayout L = pipe_layout(b, (int)sizeof(M), (int)sizeof(T), NV);
-    unsigned char *st = smem + (size_t)(i % kPipeStages) * kPipeStageBytes;
-    if (!mbar_wait_bounded(&full[i % kPipeStages], (unsigned)((i / kPipeStages) & 1)))
-      s_fail = 1;  // benign race: every writer stores 1
-    __syncthreads();
-    if (s_fail) break;
+    unsigned char *st = smem + (size_t)q * kPipeStageBytes;
+    if (!bad && !mbar_wait_bounded(&full[q], (unsigned)((i / kPipeStages) & 1))) {
+      bad = true;
+      atomicOr(plan.err, 1);
+    }
     const int *sptr = reinterpret_cast<const int *>(st);
     const int *scol = reinterpret_cast<const int *>(st + L.o_col) + (b.z - L.a_col);
     M *sval = reinterpret_cast<M *>(st + L.o_val) + (b.z - L.a_val);
@@ -391,42 +436,75 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
     if (b.y < 0 || b.y - b.x == 1) {
       // one row (or one chunk of a long row): lane l takes elements l,
       // l + 256, ... (consecutive lanes, consecutive words: no bank
-      // conflicts), sums them in a fixed order; block sum in FP64
-      M xg[kPipeMaxE];
-#pragma unroll
-      for (int u = 0; u < kPipeMaxE; ++u)
-        if (tid + u * kThreads < len) xg[u] = epi.gather(scol[tid + u * kThreads]);
+      // conflicts), sums them in a fixed order; rounds past the tile's end
+      // are left by a block-uniform break, not predicated (GB300 charges an
+      // FP64 issue slot per warp instruction however many lanes are active)
       LaneAcc<M> s;
+      if (!bad) {
+        M xg[kPipeMaxE];
 #pragma unroll
-      for (int u = 0; u < kPipeMaxE; ++u)
-        if (tid + u * kThreads < len) s.add(sval[tid + u * kThreads], xg[u]);
-      double w = warp_sum(s.total());
-      if ((tid & 31) == 0) red[tid >> 5] = w;
-      __syncthreads();
-      if (tid == 0) {
-        double tot = 0.0;
-#pragma unroll
-        for (int q = 0; q < kThreads / 32; ++q) tot += red[q];
-        if (b.y >= 0) {
-          // a row of its own: vectors from the stage
-          if constexpr (NV > 0) {
-            const T *sv0 = reinterpret_cast<const T *>(st + L.o_vec);
-            T pv[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v)
-              pv[v] = sv0[(size_t)v * (L.b_vec / sizeof(T)) + (b.x - L.a_vec)];
-            epi.row_pre(b.x, (A)tot, epi.make_pre(pv), acc);
-          } else {
-            epi.row(b.x, (A)tot, acc);
-          }
-        } else {
-          const int lid = -b.y - 1;
-          plan.lsum[t] = tot;
-          pend_prev = ticket_release(plan.lcnt + lid);
-          pend_lr = plan.lrow[lid];  // both in flight until the next tile
-          pend_lid = lid;
-          pend_row = b.x;
+        for (int u = 0; u < kPipeMaxE; ++u) {
+          if (u * kThreads >= len) break;
+          if (tid + u * kThreads < len) xg[u] = epi.gather(scol[tid + u * kThreads]);
         }
+#pragma unroll
+        for (int u = 0; u < kPipeMaxE; ++u) {
+          if (u * kThreads >= len) break;
+          if (tid + u * kThreads < len) s.add(sval[tid + u * kThreads], xg[u]);
+        }
+      }
+      // the 256 lane sums go to the stage's partials area; warp 0 adds 8
+      // per lane, then one shuffle tree (13 warp instructions, on the FP32
+      // pipe in double-float for FP32 matrices)
+      // (area of kThreads * 8 bytes: one double per lane, or for FP32 the
+      // high floats then the low floats)
+      M *ph = reinterpret_cast<M *>(st + kPipeTileBytes);
+      float *pl = reinterpret_cast<float *>(ph + kThreads);  // FP32 only
+      ph[tid] = (M)s.hi();
+      if constexpr (sizeof(M) == 4) pl[tid] = (float)s.lo();
+      consumers_sync();
+      if (warp == 0) {
+        if (!bad) {
+          LaneAcc<M> r;
+#pragma unroll
+          for (int w = 0; w < kThreads / 32; ++w) {
+            if constexpr (sizeof(M) == 4) r.add_pair(ph[lane + 32 * w], pl[lane + 32 * w]);
+            else r.add_pair(ph[lane + 32 * w], M(0));
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const M hb = __shfl_xor_sync(0xffffffffu, r.hi(), o);
+            const M lb = __shfl_xor_sync(0xffffffffu, r.lo(), o);
+            r.add_pair(hb, lb);
+          }
+          if (lane == 0) {
+            const double tot = r.total();
+            if (b.y >= 0) {
+              // a row of its own: vectors from the stage
+              if constexpr (NV > 0) {
+                const T *sv0 = reinterpret_cast<const T *>(st + L.o_vec);
+                T pv[NV];
+#pragma unroll
+                for (int v = 0; v < NV; ++v)
+                  pv[v] = sv0[(size_t)v * (L.b_vec / sizeof(T)) + (b.x - L.a_vec)];
+                epi.row_pre(b.x, (A)tot, epi.make_pre(pv), acc);
+              } else {
+                epi.row(b.x, (A)tot, acc);
+              }
+            } else {
+              const int lid = -b.y - 1;
+              plan.lsum[t] = tot;
+              pend_prev = ticket_release(plan.lcnt + lid);
+              pend_lr = plan.lrow[lid];  // both in flight until the next tile
+              pend_lid = lid;
+              pend_row = b.x;
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[q]);
+      } else if (lane == 0) {
+        mbar_arrive(&empty[q]);
       }
     } else {
       // packed rows: lane l folds the E consecutive elements [lE, lE + E)
@@ -436,10 +514,6 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
       int E = (len + kThreads - 1) / kThreads;
       E |= 1;  // <= kPipeMaxE for len <= kPipeTile
       const int beg = tid * E;
-      M xg[kPipeMaxE];
-#pragma unroll
-      for (int u = 0; u < kPipeMaxE; ++u)
-        if (u < E && beg + u < len) xg[u] = epi.gather(scol[beg + u]);
       const int r0 = b.x, R = b.y - b.x;
       const int *soff = sptr + (r0 - L.a_ptr);  // soff[j] - k0: row j's first element
       // run partials: the high part in the value slot of the run's first
@@ -447,7 +521,13 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
       // both already consumed by this lane
       float *slo = reinterpret_cast<float *>(
           reinterpret_cast<int *>(st + L.o_col) + (b.z - L.a_col));
-      if (beg < len) {
+      if (!bad && beg < len) {
+        M xg[kPipeMaxE];
+#pragma unroll
+        for (int u = 0; u < kPipeMaxE; ++u) {
+          if (u >= E) break;  // block-uniform
+          if (beg + u < len) xg[u] = epi.gather(scol[beg + u]);
+        }
         const int end = beg + E < len ? beg + E : len;
         int lo = 0, hi = R;  // row j with soff[j] - k0 <= beg < soff[j + 1] - k0
         while (hi - lo > 1) {
@@ -463,8 +543,9 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
         };
 #pragma unroll
         for (int u = 0; u < kPipeMaxE; ++u) {
+          if (u >= E) break;  // block-uniform
           const int e = beg + u;
-          if (u < E && e < end) {
+          if (e < end) {
             while (e == nb) {  // a row ends before element e
               if (segs < e) flush(segs);
               s = LaneAcc<M>();
@@ -477,17 +558,17 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
         }
         flush(segs);
       }
-      __syncthreads();
-      if (tid < R) {
+      consumers_sync();
+      if (!bad && tid < R) {
         const int a = soff[tid] - k0, e = soff[tid + 1] - k0;
         LaneAcc<M> sum;
         if (a < e) {
-          auto part_at = [&](int q) {
-            if constexpr (sizeof(M) == 4) sum.add_pair(sval[q], slo[q]);
-            else sum.add_pair(sval[q], M(0));
+          auto part_at = [&](int qq) {
+            if constexpr (sizeof(M) == 4) sum.add_pair(sval[qq], slo[qq]);
+            else sum.add_pair(sval[qq], M(0));
           };
           part_at(a);
-          for (int q = (a / E + 1) * E; q < e; q += E) part_at(q);
+          for (int qq = (a / E + 1) * E; qq < e; qq += E) part_at(qq);
         }
         if constexpr (NV > 0) {
           const T *sv0 = reinterpret_cast<const T *>(st + L.o_vec);
@@ -500,29 +581,30 @@ __global__ void __launch_bounds__(kThreads, kPipeCtasPerSm)
           epi.row(r0 + tid, (A)sum.rounded(), acc);
         }
       }
-    }
-    __syncthreads();  // the stage is free again
-    if (tid == 0 && i + kPipeStages < mine) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(i + kPipeStages);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[q]);
     }
   }
-  if (tid == 0) finish_long();
-  if (s_fail) {
-    // a copy did not complete: report, wait (bounded) for the copies still
-    // in flight into this CTA's stages, and leave
-    if (tid == 0) {
-      atomicOr(plan.err, 1);
-      for (int q = i; q < mine && q < i + kPipeStages; ++q)
-        mbar_wait_bounded(&full[q % kPipeStages], (unsigned)((q / kPipeStages) & 1));
-    }
-    return;
-  }
+  if (tid == 0 && !bad) finish_long();
   if constexpr (NF > 0) {
-    block_reduce_fields<NF, Epi::MAXMASK>(acc, red);
+    // consumers-only block reduction of the per-thread fields
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+      acc[f] = ((Epi::MAXMASK >> f) & 1u) ? warp_max(acc[f]) : warp_sum(acc[f]);
+    if (lane == 0) {
+#pragma unroll
+      for (int f = 0; f < NF; ++f) red[f * 8 + warp] = acc[f];
+    }
+    consumers_sync();
     if (tid == 0) {
 #pragma unroll
-      for (int f = 0; f < NF; ++f) part[f * G + blockIdx.x] = acc[f];
+      for (int f = 0; f < NF; ++f) {
+        double r = 0.0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w)
+          r = ((Epi::MAXMASK >> f) & 1u) ? fmax(r, red[f * 8 + w]) : r + red[f * 8 + w];
+        part[f * G + blockIdx.x] = r;
+      }
     }
   }
 }
@@ -532,7 +614,7 @@ constexpr int kPipeSmem = kPipeStages * kPipeStageBytes;
 // kPipeCtasPerSm CTAs (each with ~2 KB of static shared memory and the 1 KB
 // the SM reserves per CTA) must fit the SM's 228 KB, or the grid would run
 // in two waves.
-static_assert(kPipeCtasPerSm * (kPipeSmem + 3 * 1024) <= 228 * 1024,
+static_assert(kPipeCtasPerSm * (kPipeSmem + 2 * 1024) <= 228 * 1024,
               "pipeline stages do not fit kPipeCtasPerSm CTAs per SM");
 
 }  // namespace pdlp
