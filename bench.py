@@ -5,8 +5,9 @@ Workload (default): the 20M-nnz power-law LP -- m = 1,000,000 constraints,
 n = 2,000,000 variables, column degrees rank-Zipf(1.2) capped at 50,000, rows
 uniform within a column, values N(0,1) with 5% +-1, feasible bounds from
 x0 ~ U[0,1] (30% equality rows), 0 <= x <= 10, c ~ U[-1,1], seed 1.  Solved
-in FP64 to eps 1e-4 with the reference defaults (Ruiz 10, Pock-Chambolle 1,
-evaluation every 200 iterations), presolve off.
+to eps 1e-4 with the reference defaults (Ruiz 10, Pock-Chambolle 1,
+evaluation every 200 iterations), presolve off: FP32 PDHG with FP64
+refinement (the headline), and plain FP64 beside it.
 
 One step = one full solve (GPU rescaling, power method, PDHG loop, result).
   value : seconds per solve with the LP already resident in HBM
@@ -16,8 +17,10 @@ One step = one full solve (GPU rescaling, power method, PDHG loop, result).
 The matrices (480 MB) and vectors exceed the 129 MB L2, so no flush is
 needed between steps.
 
---impl reference times the reference algorithm's CPU restatement (the FP64
-oracle, OpenMP on every host core) on bounded samples of the same workload.
+--impl reference times the reference's own single-GPU FP64 solve (its
+cuSPARSE/cuBLAS code built from its sources for sm_103a) on the same seeded
+LP through its solve_lp_problem, one full solve per step; the FP64 oracle on
+the host cores is reported as cpu_baseline.
 """
 from __future__ import annotations
 
@@ -65,9 +68,11 @@ BATCH_WORKLOADS = {
 # n = 500,000, nnz = 5M).
 SERVE_WORKLOADS = {
     "serve_poisson_seed7": {
-        "seed": 7, "rate": 200.0, "duration": 60.0, "pool_small": 96, "pool_large": 4,
-        "desc": "Poisson arrivals (seed 7); requests from the batch distribution with 10% "
-                "large LPs (m=200,000 n=500,000 nnz=5M), FP64, eps 1e-4",
+        "seed": 7, "rate": 200.0, "duration": 60.0, "pool_small": 2000, "pool_large": 50,
+        "queue_bytes": 4 << 30,
+        "desc": "Poisson arrivals at 200/s for 60 s (seed 7); each request an LP from the "
+                "batch distribution (m log-uniform in [1e3, 1e5], n = 2.5 m, 10 nnz per "
+                "column), 10% of them large (m=200,000 n=500,000 nnz=5M), eps 1e-4",
     },
 }
 
@@ -289,8 +294,11 @@ def run_ours(args, cp, rank, world, local):
     prec = {"fp32": cp.PRECISION_FP32_REFINE, "fp32m": cp.PRECISION_FP32_MATRIX,
             "fp64": cp.PRECISION_FP64}[args.precision]
     dp = cp.DeviceProblem(prob)
-    for _ in range(args.warmup):
+    first_info = {}
+    for i in range(args.warmup):
         out = dp.solve(params, precision=prec)
+        if i == 0:
+            first_info = out.info
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -329,7 +337,18 @@ def run_ours(args, cp, rank, world, local):
                     "status": f_last.result["status"],
                     "primal_obj": f_last.result["primal_objective_value"],
                     "us_per_iteration": round(f_last.info["loop_seconds"] /
-                                              max(1, f_last.result["total_count"]) * 1e6, 2)}
+                                              max(1, f_last.result["total_count"]) * 1e6, 2),
+                    "speedup_of_headline": round(statistics.mean(f_dev) / statistics.mean(dev_s),
+                                                 3)}
+            # error of the headline result against the FP64 solve (whose
+            # iterates equal the reference's on the configured LPs)
+            a, b = last.result, f_last.result
+            rel = lambda u, v: abs(u - v) / (1.0 + abs(v))
+            vrel = lambda u, v: float(abs(u - v).max() / (1.0 + abs(v).max())) if len(v) else 0.0
+            fp64["error_of_headline_vs_fp64"] = {
+                "primal_obj_rel": rel(a["primal_objective_value"], b["primal_objective_value"]),
+                "dual_obj_rel": rel(a["dual_objective_value"], b["dual_objective_value"]),
+                "x_rel_max": vrel(a["x"], b["x"]), "y_rel_max": vrel(a["y"], b["y"])}
     clocks = clk.summary()
     value, e2e_mean = max_over_ranks([statistics.mean(dev_s), statistics.mean(e2e_s)])
     r = last.result
@@ -385,6 +404,12 @@ def run_ours(args, cp, rank, world, local):
                      "timing": timing,
                      "isolated_ms": {"primal_step": round(ms[0], 4), "dual_step": round(ms[1], 4),
                                      "eval_A": round(ms[2], 4), "eval_AT": round(ms[3], 4)}},
+        "spmv_kernels": {"A": ["fused", "pipelined"][out.info["spmv_kernel_A"]],
+                         "A^T": ["fused", "pipelined"][out.info["spmv_kernel_AT"]],
+                         "chosen_by": "timing both on the step kernels at the problem's first "
+                                      "solve (ms per launch: A fused, A pipelined, A^T fused, "
+                                      "A^T pipelined)",
+                         "tune_ms": [round(v, 4) for v in first_info.get("tune_ms", [])]},
         "solve": {"status": r["status"], "iterations": iters, "power_iterations": pm_iters,
                   "rel_primal": r["relative_primal_residual"],
                   "rel_dual": r["relative_dual_residual"], "rel_gap": r["relative_objective_gap"],
@@ -498,15 +523,18 @@ def run_batch(args, cp):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     if oracle_lib.ref_gpu_available() and gpu_visible():
-        t0, k = time.perf_counter(), 0
+        t0, k, solve_s = time.perf_counter(), 0, 0.0
         try:
             while k < count and time.perf_counter() - t0 < args.ref_seconds:
-                oracle_lib.ref_gpu_solve(lps[k], eps=args.eps, timeout=600)
+                solve_s += oracle_lib.ref_gpu_solve(lps[k], eps=args.eps, timeout=600)["wall_s"]
                 k += 1
             el = time.perf_counter() - t0
-            ref_seq = {"lps_per_second": round(k / el, 3), "lps": k, "seconds": round(el, 2),
+            ref_seq = {"lps_per_second": round(k / solve_s, 3), "lps": k,
+                       "solve_seconds": round(solve_s, 2), "process_seconds": round(el, 2),
                        "api": "the reference's solve_lp_problem (single-GPU FP64 build), one "
-                              "process per LP, the first LPs of the batch in order"}
+                              "process per LP, the first LPs of the batch in order; LPs/s "
+                              "over the solve_lp_problem calls alone (process start and CUDA "
+                              "context creation excluded)"}
         except (RuntimeError, OSError) as e:
             ref_seq = {"unavailable": str(e)[:200]}
     cpu = None
@@ -553,8 +581,14 @@ def run_batch(args, cp):
 
 
 def run_serve(args, cp):
-    """Open-loop serving: requests arrive by a Poisson process; latency runs
-    from the scheduled arrival to the result on the host."""
+    """Open-loop serving: requests arrive by a Poisson process at the
+    configured rate for the configured window; latency runs from the
+    scheduled arrival to the result on the host.  The server's queue is
+    bounded in host memory, so under a load above the GPU's capacity the
+    backlog stays bounded and the requests it cannot take are refused and
+    counted.  Each request is drawn from a pool of distinct seeded LPs
+    generated before the run (new LPs at 200/s cannot be generated on the
+    host's cores while it serves)."""
     import numpy as np
     w = SERVE_WORKLOADS[args.workload]
     rate = args.rate or w["rate"]
@@ -562,7 +596,9 @@ def run_serve(args, cp):
     rng = np.random.default_rng(w["seed"])
     shapes = batch_shapes(w["pool_small"], 7000)
     shapes += [(200000, 500000, 5000000, 8000 + i) for i in range(w["pool_large"])]
+    tg = time.perf_counter()
     pool = generate_parallel(cp, shapes)
+    gen_s = time.perf_counter() - tg
     arrivals, t = [], 0.0
     while True:
         t += rng.exponential(1.0 / rate)
@@ -577,6 +613,7 @@ def run_serve(args, cp):
     import threading
     lat, done_t = [None] * len(arrivals), [None] * len(arrivals)
     with cp.Server(params, precision=prec, workers=args.workers) as srv:
+        srv.set_queue_limit(w["queue_bytes"])
         ids = [None] * len(arrivals)
         t0 = time.perf_counter()
 
@@ -584,7 +621,9 @@ def run_serve(args, cp):
             for k in range(len(arrivals)):
                 while ids[k] is None:
                     time.sleep(0.0005)
-                res, info = srv.wait(ids[k])
+                if ids[k] < 0:
+                    continue
+                srv.wait(ids[k])
                 done_t[k] = time.perf_counter() - t0
                 lat[k] = done_t[k] - arrivals[k][0]
 
@@ -599,24 +638,32 @@ def run_serve(args, cp):
             th.join()
         st = srv.stats()
     clocks = clk.summary()
-    total = max(done_t)
-    lat_ms = np.array(lat) * 1e3
+    served = [k for k in range(len(arrivals)) if lat[k] is not None]
+    total = max(done_t[k] for k in served)
+    lat_ms = np.array([lat[k] for k in served]) * 1e3
+    large_ms = np.array([lat[k] for k in served if arrivals[k][1] >= w["pool_small"]]) * 1e3
     line = {
-        "metric": "served LPs/s; p50/p99 latency", "value": round(len(arrivals) / total, 2),
+        "metric": "served LPs/s; p50/p99 latency", "value": round(len(served) / total, 2),
         "unit": "LPs/s", "n_gpus": 1, "steps": 1, "warmup": 0,
         "ms_per_step": round(total * 1e3, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": args.workload, "description": w["desc"], "rate_per_s": rate,
-                   "precision": args.precision,
-                   "duration_s": duration, "requests": len(arrivals), "workers": args.workers,
-                   "pool": f"{w['pool_small']} batch-distribution LPs + {w['pool_large']} large",
-                   "eps": args.eps},
+                   "precision": args.precision, "duration_s": duration,
+                   "requests": len(arrivals), "workers": args.workers,
+                   "pool": f"{w['pool_small']} + {w['pool_large']} distinct LPs generated "
+                           f"before the run ({gen_s:.1f} s)",
+                   "queue_bound_host_bytes": w["queue_bytes"], "eps": args.eps},
         "latency_ms": {"p50": round(float(np.percentile(lat_ms, 50)), 2),
                        "p99": round(float(np.percentile(lat_ms, 99)), 2),
                        "mean": round(float(lat_ms.mean()), 2),
-                       "max": round(float(lat_ms.max()), 2)},
-        "e2e": {"value": round(len(arrivals) / total, 2), "unit": "LPs/s",
+                       "max": round(float(lat_ms.max()), 2),
+                       "large_p50": round(float(np.percentile(large_ms, 50)), 2)
+                       if len(large_ms) else None},
+        "requests": {"arrived": len(arrivals), "served": len(served),
+                     "refused_by_queue_bound": int(st["rejected"]),
+                     "offered_rate_per_s": round(len(arrivals) / duration, 1)},
+        "e2e": {"value": round(len(served) / total, 2), "unit": "LPs/s",
                 "api": "pdlp_server_submit / pdlp_server_wait from host arrays"},
         "server": {"completed": st["completed"], "failed": st["failed"],
                    "max_in_flight": st["max_in_flight"], "iterations": st["iterations"]},
@@ -744,8 +791,8 @@ def main():
     ap.add_argument("--precision", choices=["fp32", "fp32m", "fp64"], default=None,
                     help="fp32: FP32 iterates + FP64 refinement; fp32m: FP32 matrix "
                          "and SpMVs with FP64 iterates + FP64 refinement; fp64: plain FP64 "
-                         "(default: fp64 for single solves, fp32 for the batch and serving "
-                         "workloads, as their configurations specify)")
+                         "(default: fp32, the metric's headline; single solves report the "
+                         "FP64 solve beside it)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time the iteration kernels alone and exit (a short command for "
                          "profilers; prints no bench line)")
@@ -754,8 +801,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.precision is None:
-        many = args.workload in BATCH_WORKLOADS or args.workload in SERVE_WORKLOADS
-        args.precision = "fp32" if many else "fp64"
+        # the metric is FP32 + FP64 refinement against FP64: the headline is
+        # the FP32 + refinement solve, with the FP64 solve beside it
+        args.precision = "fp32"
     os.environ.setdefault("PDLP_QUIET", "1")
     rank, world, local = rank_info()
     if world > 1:

@@ -328,6 +328,9 @@ cupdlpx_result_t *run_solve(const pdlp::DevProblem &P, const pdhg_parameters_t &
     info->primal_step_ms = s.live_primal_ms();
     info->dual_step_ms = s.live_dual_ms();
     info->timed_chunks = s.live_samples();
+    info->spmv_kernel_A = s.pipe_A() ? 1 : 0;
+    info->spmv_kernel_AT = s.pipe_AT() ? 1 : 0;
+    for (int i = 0; i < 4; ++i) info->tune_ms[i] = s.tune_ms(i);
   }
   return r;
 }
@@ -364,6 +367,9 @@ cupdlpx_result_t *run_refined(const pdlp::DevProblem &P, const pdhg_parameters_t
     info->precision = o.precision;
     info->timed_chunks = rep.timed_chunks;
     info->fp64_finish = rep.fp64_finish ? 1 : 0;
+    info->spmv_kernel_A = rep.kernel_A;
+    info->spmv_kernel_AT = rep.kernel_AT;
+    for (int q = 0; q < 4; ++q) info->tune_ms[q] = rep.tune_ms[q];
     if (rep.timed_chunks > 0) {
       info->primal_step_ms = rep.timed_primal_ms_sum / rep.timed_chunks;
       info->dual_step_ms = rep.timed_dual_ms_sum / rep.timed_chunks;

@@ -370,14 +370,17 @@ __device__ __forceinline__ void set_steps(Ctl *c) {
   c->inv_sigma = 1.0 / c->sigma;
 }
 
-// Every SpMV of a solve runs the pipelined kernel when its matrix has a pipe
-// plan (and PDLP_STEP_KERNEL is not "fused"), else the fused kernel; the
-// sites' reduction partials follow the kernel that writes them.
-bool pipe_enabled();
+// Each matrix of a solve runs every SpMV on one of the two kernels: the
+// pipelined one (M.pipe_on) or the fused one.  The choice is made per matrix
+// by timing both on the step epilogue (Solve::tune_kernels), or forced by
+// PDLP_STEP_KERNEL=pipe / fused; reduction partials are sized for either
+// and folded with the counts of the kernel in use.
+// 1: forced pipelined, 0: forced fused, -1: measured per matrix
+int kernel_override();
 
 template <class V>
 inline bool use_pipe(const DevCsrT<V> &M) {
-  return M.pipe.ntile > 0 && pipe_enabled();
+  return M.pipe_on && M.pipe.ntile > 0;
 }
 template <class V>
 inline size_t spmv_partials(const DevCsrT<V> &M) {
@@ -386,6 +389,15 @@ inline size_t spmv_partials(const DevCsrT<V> &M) {
 template <class V>
 inline size_t spmv_long_rows(const DevCsrT<V> &M) {
   return use_pipe(M) ? (size_t)M.pipe.nlong : (size_t)M.plan.nlong;
+}
+// partial buffers large enough for either kernel
+template <class V>
+inline size_t spmv_partials_max(const DevCsrT<V> &M) {
+  return (size_t)(M.pipe.grid > M.plan.nblk ? M.pipe.grid : M.plan.nblk);
+}
+template <class V>
+inline size_t spmv_long_rows_max(const DevCsrT<V> &M) {
+  return (size_t)(M.pipe.nlong > M.plan.nlong ? M.pipe.nlong : M.plan.nlong);
 }
 
 template <class Epi>

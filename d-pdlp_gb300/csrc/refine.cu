@@ -293,6 +293,9 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
       s.enable_snapshot();
       s.run();
       if (round == 0) {
+        rep.kernel_A = s.pipe_A() ? 1 : 0;
+        rep.kernel_AT = s.pipe_AT() ? 1 : 0;
+        for (int q = 0; q < 4; ++q) rep.tune_ms[q] = s.tune_ms(q);
         omega0 = s.primal_weight();
         cb0 = s.cb();
         ob0 = s.ob();

@@ -56,10 +56,17 @@ lp_problem_t *copy_problem(const lp_problem_t *p) {
   return q;
 }
 
+// Host bytes of a problem's copy (CSR and vectors).
+long long host_bytes(const lp_problem_t *p) {
+  return 12LL * p->constraint_matrix_num_nonzeros + 4LL * (p->num_constraints + 1) +
+         8LL * (3LL * p->num_variables + 2LL * p->num_constraints);
+}
+
 struct Request {
   long long id = 0;
   lp_problem_t *prob = nullptr;
   long long bytes = 0;
+  long long host = 0;  // host bytes of the queued copy
   Clock::time_point submitted, admitted, finished;
   cupdlpx_result_t *result = nullptr;
   int worker = -1;
@@ -80,6 +87,9 @@ struct pdlp_server {
   std::deque<std::shared_ptr<Request>> queue;
   std::map<long long, std::shared_ptr<Request>> requests;
   long long next_id = 0, in_use = 0;
+  // queue bound: requests whose copies would take the waiting requests past
+  // queue_limit host bytes are refused (0: no bound)
+  long long queue_limit = 0, queued_host = 0, rejected = 0;
   int in_flight = 0, max_in_flight = 0;
   long long completed = 0, failed = 0, iterations = 0;
   bool stopping = false;
@@ -103,6 +113,7 @@ struct pdlp_server {
         if (queue.empty()) break;  // stopping and drained
         r = queue.front();
         queue.pop_front();
+        queued_host -= r->host;
         in_use += r->bytes;
         ++in_flight;
         if (in_flight > max_in_flight) max_in_flight = in_flight;
@@ -206,16 +217,34 @@ pdlp_server_t *pdlp_server_create(const pdhg_parameters_t *params, const pdlp_op
 
 long long pdlp_server_submit(pdlp_server_t *s, const lp_problem_t *prob) {
   if (!s || !prob) return -1;
+  const long long hb = host_bytes(prob);
+  const auto submitted = Clock::now();
+  {
+    // reserve the copy's bytes in the queue, or refuse the request
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->queue_limit > 0 && !s->queue.empty() && s->queued_host + hb > s->queue_limit) {
+      ++s->rejected;
+      pdlp::record_error("pdlp_server_submit: queue full (host-byte limit reached)");
+      return -2;
+    }
+    s->queued_host += hb;
+  }
   lp_problem_t *q = copy_problem(prob);
-  if (!q) return -1;
+  if (!q) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->queued_host -= hb;
+    return -1;
+  }
   auto r = std::make_shared<Request>();
   r->prob = q;
+  r->host = hb;
   r->bytes = pdlp_estimate_device_bytes(q->num_constraints, q->num_variables,
                                         q->constraint_matrix_num_nonzeros, s->opts.precision);
-  r->submitted = Clock::now();
+  r->submitted = submitted;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stopping) {
+      s->queued_host -= hb;
       lp_problem_free(q);
       return -1;
     }
@@ -265,6 +294,15 @@ int pdlp_server_stats(pdlp_server_t *s, pdlp_server_stats_t *out) {
   out->iterations = s->iterations;
   out->device_bytes_in_use = s->in_use;
   out->busy_seconds = s->any_admitted ? since(s->first_admit, s->last_finish) : 0.0;
+  out->rejected = s->rejected;
+  out->queued_host_bytes = s->queued_host;
+  return 0;
+}
+
+int pdlp_server_set_queue_limit(pdlp_server_t *s, long long max_queued_host_bytes) {
+  if (!s || max_queued_host_bytes < 0) return -1;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->queue_limit = max_queued_host_bytes;
   return 0;
 }
 

@@ -162,14 +162,14 @@ static int pick_chunk(int tile) {
   return tile * 8 < 8192 ? tile * 8 : 8192;
 }
 
-// The SpMVs of a solve use the pipelined kernel when PDLP_STEP_KERNEL=pipe,
-// else the fused kernel.
-bool pipe_enabled() {
-  static const bool on = [] {
+int kernel_override() {
+  static const int v = [] {
     const char *e = getenv("PDLP_STEP_KERNEL");
-    return e && strcmp(e, "pipe") == 0;
+    if (e && strcmp(e, "pipe") == 0) return 1;
+    if (e && strcmp(e, "fused") == 0) return 0;
+    return -1;
   }();
-  return on;
+  return v;
 }
 
 DevProblem::~DevProblem() {

@@ -9,6 +9,7 @@
 
 #include <array>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <new>
 #include <string>
@@ -31,6 +32,7 @@ struct DevCsrT {
   T *val = nullptr;
   SpmvPlan plan;
   PipePlan pipe;
+  bool pipe_on = false;  // this matrix's SpMVs run on the pipelined kernel
 };
 using DevCsr = DevCsrT<double>;
 
@@ -158,6 +160,11 @@ struct DevProblem {
   // (pdlp_device_problem_t) switches to the per-thread stream: its solves
   // return only after their work on the problem has finished.
   cudaStream_t owner = cudaStreamPerThread;
+  // SpMV kernel per matrix and precision (index: 0 FP64, 1 FP32, 2 FP32
+  // matrix), measured by the first solve of each precision: -1 not yet
+  // measured, 0 fused, 1 pipelined; {A, A^T}
+  mutable int kernel_choice[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+  mutable std::mutex tune_mu;
   ~DevProblem();
 };
 
@@ -282,6 +289,23 @@ class Solve {
   void read_timing(int slot);
   void power_method();
   void check_pipe_errors() const;
+  // kernel choice per matrix: apply (pipe_A, pipe_T) to the matrices and the
+  // fold counts; tune_kernels times both kernels on the step epilogues
+  void apply_kernels(bool pipe_A, bool pipe_T);
+  void tune_kernels();
+  int precision_index() const { return sizeof(T) == 4 ? 1 : sizeof(M) == 4 ? 2 : 0; }
+  bool tuned_ = false;
+
+ public:
+  // kernels per matrix after tuning (pipelined or not) and the tuning's
+  // measured ms per launch: {A fused, A pipelined, A^T fused, A^T pipelined}
+  // (zeros when the choice came from the problem's cache or an override)
+  bool pipe_A() const { return A64_.pipe_on; }
+  bool pipe_AT() const { return AT64_.pipe_on; }
+  double tune_ms(int i) const { return tune_ms_[i]; }
+
+ private:
+  double tune_ms_[4] = {0, 0, 0, 0};
 
   pdhg_parameters_t p_;
   cudaStream_t st_;
@@ -367,6 +391,8 @@ struct RefineOptions {
 };
 
 struct RefineReport {
+  int kernel_A = 0, kernel_AT = 0;  // SpMV kernels of the FP32 rounds (1: pipelined)
+  double tune_ms[4] = {0, 0, 0, 0};
   int rounds = 0;
   int power_iterations = 0;
   double sigma_max = 0.0;

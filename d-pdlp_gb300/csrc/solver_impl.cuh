@@ -464,8 +464,8 @@ void Solve<T, M>::alloc() {
   const size_t vn = n, vm = m;
   // reduction partials of an SpMV site: one per CTA of the pipelined kernel
   // (or per block of the fused kernel) plus one per long row
-  const size_t nbA = spmv_partials(P_.A), nbT = spmv_partials(P_.AT);
-  const size_t nlA = spmv_long_rows(P_.A), nlT = spmv_long_rows(P_.AT);
+  const size_t nbA = spmv_partials_max(P_.A), nbT = spmv_partials_max(P_.AT);
+  const size_t nlA = spmv_long_rows_max(P_.A), nlT = spmv_long_rows_max(P_.AT);
   Sizer z;
   z.add<double>(nnz); z.add<double>(nnz);                      // FP64 scaled values
   if (!M64) { z.add<M>(nnz); z.add<M>(nnz); }                  // iteration values
@@ -592,9 +592,83 @@ void Solve<T, M>::alloc() {
   pw_.m = m;
   pw_.ctl = d.ctl;
   pw_.hflag = dflag;
-  pw_.nblkA = (int)nbA;
-  pw_.nlongA = (int)nlA;
   pw_.ew_grid = ew;
+  // kernels: the problem's measured choice for this precision, a forced one,
+  // or the fused kernel until run() measures both
+  int cA = 0, cT = 0;
+  {
+    std::lock_guard<std::mutex> lk(P_.tune_mu);
+    const int *ch = P_.kernel_choice[precision_index()];
+    if (kernel_override() >= 0) {
+      cA = cT = kernel_override();
+      tuned_ = true;
+    } else if (ch[0] >= 0 && ch[1] >= 0) {
+      cA = ch[0];
+      cT = ch[1];
+      tuned_ = true;
+    }
+  }
+  apply_kernels(cA != 0, cT != 0);
+}
+
+template <class T, class M>
+void Solve<T, M>::apply_kernels(bool pipe_A, bool pipe_T) {
+  Dev<T> &d = d_;
+  A64_.pipe_on = A_.pipe_on = pipe_A && P_.A.pipe.ntile > 0;
+  AT64_.pipe_on = AT_.pipe_on = pipe_T && P_.AT.pipe.ntile > 0;
+  d.nblkA = (int)spmv_partials(A64_);
+  d.nlongA = (int)spmv_long_rows(A64_);
+  d.nblkT = (int)spmv_partials(AT64_);
+  d.nlongT = (int)spmv_long_rows(AT64_);
+  pw_.nblkA = d.nblkA;
+  pw_.nlongA = d.nlongA;
+}
+
+// The SpMV kernel of each matrix, measured once per problem and precision:
+// the step kernel of the matrix (primal step over A^T, dual step over A) on
+// both kernels, 2 warm and 5 timed launches each, CUDA events on the solve's
+// stream; the pipelined kernel is kept where it is at least 3% faster.
+// Runs before the first iteration (the step kernels only write the next
+// iterates and x_ref, which the loop writes before it reads them).
+template <class T, class M>
+void Solve<T, M>::tune_kernels() {
+  if (tuned_) return;
+  tuned_ = true;
+  std::lock_guard<std::mutex> lk(P_.tune_mu);
+  int *ch = P_.kernel_choice[precision_index()];
+  if (ch[0] < 0 || ch[1] < 0) {
+    Dev<T> &d = d_;
+    cudaEvent_t e0, e1;
+    PDLP_CUDA(cudaEventCreate(&e0));
+    PDLP_CUDA(cudaEventCreate(&e1));
+    auto timed = [&](auto &&launch) {
+      for (int i = 0; i < 2; ++i) launch();
+      PDLP_CUDA(cudaEventRecord(e0, st_));
+      for (int i = 0; i < 5; ++i) launch();
+      PDLP_CUDA(cudaEventRecord(e1, st_));
+      PDLP_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      PDLP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    PrimalEpi<T, M, false, false, true> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
+    DualEpi<T, M, false, false, true> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
+    float tf[2] = {0.f, 0.f}, tp[2] = {0.f, 0.f};
+    for (int k = 0; k < 2; ++k) {
+      apply_kernels(k != 0, k != 0);
+      float a = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
+      float t = timed([&] { launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_); });
+      (k ? tp : tf)[0] = a;
+      (k ? tp : tf)[1] = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ch[0] = P_.A.pipe.ntile > 0 && tp[0] < 0.97f * tf[0] ? 1 : 0;
+    ch[1] = P_.AT.pipe.ntile > 0 && tp[1] < 0.97f * tf[1] ? 1 : 0;
+    tune_ms_[0] = tf[0] / 5; tune_ms_[1] = tp[0] / 5;
+    tune_ms_[2] = tf[1] / 5; tune_ms_[3] = tp[1] / 5;
+  }
+  apply_kernels(ch[0] != 0, ch[1] != 0);
 }
 
 template <class T, class M>
@@ -774,18 +848,25 @@ void Solve<T, M>::init_step(double known_sigma, double known_omega) {
 template <class T, class M>
 void Solve<T, M>::enqueue_eval(int off, bool infeas, bool restart_check, int mode) {
   Dev<T> &d = d_;
+  // KKT evaluation on the FP64 scaled matrix in every precision: an FP32
+  // round then stops when the FP64 KKT of its own point meets the tolerance,
+  // not when rounding in long cancelling rows lets it (evaluations are about
+  // 1% of the SpMVs)
   if (d.linf) {
-    launch_spmv(A_, EvalAEpi<T, M, true>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<T, M, true>{d}, d.p_e2, d.lp_e2, st_);
+    launch_spmv(A64_, EvalAEpi<T, double, true>{d}, d.p_e1, d.lp_e1, st_);
+    launch_spmv(AT64_, EvalATEpi<T, double, true>{d}, d.p_e2, d.lp_e2, st_);
   } else {
-    launch_spmv(A_, EvalAEpi<T, M, false>{d}, d.p_e1, d.lp_e1, st_);
-    launch_spmv(AT_, EvalATEpi<T, M, false>{d}, d.p_e2, d.lp_e2, st_);
+    launch_spmv(A64_, EvalAEpi<T, double, false>{d}, d.p_e1, d.lp_e1, st_);
+    launch_spmv(AT64_, EvalATEpi<T, double, false>{d}, d.p_e2, d.lp_e2, st_);
   }
   if (infeas) {
+    // the ray statistics likewise on the FP64 matrix: the infeasibility test
+    // compares them with eps_infeasible (1e-10 by default), below what FP32
+    // sums over long rows resolve
     k_ray_project<T><<<d.ew_grid, kThreads, 0, st_>>>(d);
     k_ray_project_fin<T><<<1, kThreads, 0, st_>>>(d);
-    launch_spmv(A_, InfAEpi<T, M>{d, T(0)}, d.p_i1, d.lp_i1, st_);
-    launch_spmv(AT_, InfATEpi<T, M>{d, T(0)}, d.p_i2, d.lp_i2, st_);
+    launch_spmv(A64_, InfAEpi<T, double>{d, T(0)}, d.p_i1, d.lp_i1, st_);
+    launch_spmv(AT64_, InfATEpi<T, double>{d, T(0)}, d.p_i2, d.lp_i2, st_);
   }
   k_eval_fin<T><<<1, kThreads, 0, st_>>>(d, off, infeas, restart_check, mode);
   PDLP_LAUNCH_CHECK();
@@ -978,6 +1059,7 @@ void Solve<T, M>::run() {
   Dev<T> &d = d_;
   const int L = p_.termination_criteria.iteration_limit;
   const int CH = 100;
+  tune_kernels();
   auto t0 = std::chrono::steady_clock::now();
   k_loop_start<<<1, 1, 0, st_>>>(d.ctl);
   PDLP_LAUNCH_CHECK();
@@ -1172,8 +1254,8 @@ void Solve<T, M>::time_kernels(int reps, double *ms) {
   DualEpi<T, M, false, false, true> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
   ms[0] = timed([&] { launch_spmv(AT_, pe, nullptr, nullptr, st_); });
   ms[1] = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
-  ms[2] = timed([&] { launch_spmv(A_, EvalAEpi<T, M, false>{d}, d.p_e1, d.lp_e1, st_); });
-  ms[3] = timed([&] { launch_spmv(AT_, EvalATEpi<T, M, false>{d}, d.p_e2, d.lp_e2, st_); });
+  ms[2] = timed([&] { launch_spmv(A64_, EvalAEpi<T, double, false>{d}, d.p_e1, d.lp_e1, st_); });
+  ms[3] = timed([&] { launch_spmv(AT64_, EvalATEpi<T, double, false>{d}, d.p_e2, d.lp_e2, st_); });
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
 }

@@ -61,10 +61,10 @@ namespace pdlp {
 #define PDLP_PIPE_TILE 2048
 #endif
 #ifndef PDLP_PIPE_STAGES
-#define PDLP_PIPE_STAGES 3
+#define PDLP_PIPE_STAGES 2
 #endif
 #ifndef PDLP_PIPE_CTAS
-#define PDLP_PIPE_CTAS 2
+#define PDLP_PIPE_CTAS 3
 #endif
 constexpr int kPipeRows = kThreads;      // rows per packed tile (one per thread)
 constexpr int kPipeTile = PDLP_PIPE_TILE;

@@ -179,10 +179,22 @@ class SolveInfo(C.Structure):
         ("dual_step_ms", C.c_double),
         ("timed_chunks", C.c_int),
         ("fp64_finish", C.c_int),
+        ("spmv_kernel_A", C.c_int),
+        ("spmv_kernel_AT", C.c_int),
+        ("tune_ms", C.c_double * 4),
     ]
 
 
 PRECISION_FP64, PRECISION_FP32_REFINE, PRECISION_FP32_MATRIX = 0, 1, 2
+
+
+def info_dict(info) -> dict:
+    """pdlp_solve_info_t as a dict (arrays as lists)."""
+    out = {}
+    for f, _ in SolveInfo._fields_:
+        v = getattr(info, f)
+        out[f] = list(v) if hasattr(v, "__len__") else v
+    return out
 
 
 class RequestInfo(C.Structure):
@@ -196,7 +208,8 @@ class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_longlong), ("failed", C.c_longlong),
                 ("queued", C.c_longlong), ("in_flight", C.c_int), ("max_in_flight", C.c_int),
                 ("iterations", C.c_longlong), ("device_bytes_in_use", C.c_longlong),
-                ("busy_seconds", C.c_double)]
+                ("busy_seconds", C.c_double), ("rejected", C.c_longlong),
+                ("queued_host_bytes", C.c_longlong)]
 
 
 class BatchInfo(C.Structure):
@@ -299,6 +312,8 @@ def _declare_ext(lib: C.CDLL) -> None:
     lib.pdlp_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(RequestInfo)]
     lib.pdlp_server_stats.restype = C.c_int
     lib.pdlp_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.pdlp_server_set_queue_limit.restype = C.c_int
+    lib.pdlp_server_set_queue_limit.argtypes = [C.c_void_p, C.c_longlong]
     lib.pdlp_server_destroy.restype = None
     lib.pdlp_server_destroy.argtypes = [C.c_void_p]
     lib.pdlp_batch_solve.restype = C.c_int
@@ -498,7 +513,7 @@ def solve(problem: Problem, params: PdhgParameters | None = None, trace_cap: int
         finally:
             L.cupdlpx_result_free(r)
         return SolveOutput(res, np.zeros((0, TRACE_WIDTH)),
-                           {f: getattr(info, f) for f, _ in SolveInfo._fields_})
+                           info_dict(info))
     tr = np.zeros((max(trace_cap, 1), TRACE_WIDTH))
     tl = C.c_int(0)
     info = SolveInfo()
@@ -511,7 +526,7 @@ def solve(problem: Problem, params: PdhgParameters | None = None, trace_cap: int
         res = result_dict(r)
     finally:
         L.cupdlpx_result_free(r)
-    inf = {f: getattr(info, f) for f, _ in SolveInfo._fields_}
+    inf = info_dict(info)
     return SolveOutput(res, tr[: tl.value].copy(), inf)
 
 
@@ -541,7 +556,7 @@ class DeviceProblem:
         finally:
             self._lib.cupdlpx_result_free(r)
         return SolveOutput(res, np.zeros((0, TRACE_WIDTH)),
-                           {f: getattr(info, f) for f, _ in SolveInfo._fields_})
+                           info_dict(info))
 
     def time_kernels(self, params: PdhgParameters | None = None, reps: int = 20,
                      precision: int = PRECISION_FP64) -> np.ndarray:
@@ -578,10 +593,17 @@ class Server:
             raise RuntimeError("server creation failed: " + self._lib.pdlp_last_error().decode())
 
     def submit(self, problem: Problem) -> int:
+        """Request id, or -2 when the queue bound refused the request."""
         rid = self._lib.pdlp_server_submit(self.handle, problem.ptr)
+        if rid == -2:
+            return -2
         if rid < 0:
             raise RuntimeError("submit failed")
         return rid
+
+    def set_queue_limit(self, host_bytes: int) -> None:
+        if self._lib.pdlp_server_set_queue_limit(self.handle, host_bytes) != 0:
+            raise ValueError("bad queue limit")
 
     def submit_bytes(self, payload: bytes) -> int:
         rid = self._lib.pdlp_server_submit_bytes(self.handle, payload, len(payload))

@@ -42,6 +42,13 @@ typedef struct {
   int timed_chunks;           /* chunks those averages cover (0: none) */
   int fp64_finish;            /* 1 when a mixed-precision solve ended with FP64
                                  PDHG warm-started from its best FP64 point */
+  int spmv_kernel_A;          /* SpMV kernel of A (dual step and its other
+                                 products): 0 fused, 1 pipelined */
+  int spmv_kernel_AT;         /* the same for A^T (primal step) */
+  double tune_ms[4];          /* the measurement that chose them, ms per
+                                 launch: A fused, A pipelined, A^T fused, A^T
+                                 pipelined (zeros when the choice was reused
+                                 from an earlier solve of the problem) */
 } pdlp_solve_info_t;
 
 /* Arithmetic of the PDHG iteration.
@@ -159,6 +166,8 @@ typedef struct {
   long long iterations;     /* PDHG iterations summed over finished requests */
   long long device_bytes_in_use; /* footprint of the requests in flight */
   double busy_seconds;      /* first admission to last finish */
+  long long rejected;       /* submissions refused by the queue bound */
+  long long queued_host_bytes; /* host bytes of the waiting requests' copies */
 } pdlp_server_stats_t;
 
 /* Estimated device bytes of one solve (problem plus solve workspace). */
@@ -167,8 +176,15 @@ long long pdlp_estimate_device_bytes(int m, int n, long long nnz, int precision)
 pdlp_server_t *pdlp_server_create(const pdhg_parameters_t *params,
                                   const pdlp_options_t *opts, int workers,
                                   long long mem_budget_bytes);
-/* Queue a copy of prob; returns the request id (>= 0) or -1. */
+/* Queue a copy of prob; returns the request id (>= 0), -1 on failure, or
+ * -2 when the queue bound refuses it (pdlp_server_set_queue_limit). */
 long long pdlp_server_submit(pdlp_server_t *s, const lp_problem_t *prob);
+/* Bound the queue: a submission whose copy would take the requests waiting
+ * for admission past max_queued_host_bytes of host memory is refused (-2)
+ * unless the queue is empty; 0 (the default) removes the bound.  Under an
+ * arrival rate above the GPU's capacity this keeps the host memory of the
+ * backlog bounded; refused requests are counted in the stats. */
+int pdlp_server_set_queue_limit(pdlp_server_t *s, long long max_queued_host_bytes);
 /* Block until request `id` is solved; the result (NULL on failure, see
  * pdlp_last_error) belongs to the caller; info may be NULL.  Each id can be
  * collected once. */

@@ -118,3 +118,21 @@ def test_wire_payloads_solve_like_problems():
         got = [srv.wait(i)[0] for i in ids]
     for lp, g in zip(lps, got):
         _same(cp.solve(lp, p).result, g)
+
+
+def test_queue_bound_refuses_and_accepted_requests_equal_alone():
+    # one worker and a 1-byte bound: a request is queued only when nothing
+    # waits, so a burst of submissions is partly refused (-2, counted); every
+    # accepted request still completes, bitwise as alone
+    lps = _mixed_lps(10, seed0=500)
+    p = _params()
+    with cp.Server(p, workers=1) as srv:
+        srv.set_queue_limit(1)
+        ids = [srv.submit(lp) for lp in lps]
+        results = {k: srv.wait(rid)[0] for k, rid in enumerate(ids) if rid >= 0}
+        st = srv.stats()
+    refused = sum(1 for rid in ids if rid == -2)
+    assert refused >= 1 and st["rejected"] == refused
+    assert len(results) == 10 - refused and st["queued_host_bytes"] == 0
+    for k, res in results.items():
+        _same(res, cp.solve(lps[k], p).result)
