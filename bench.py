@@ -222,14 +222,16 @@ def kernel_bytes(m, n, nnz, s=8):
     return primal, dual
 
 
-def load_traffic(workload, kernel):
+def load_traffic(workload, precision, kernel):
+    """DRAM bytes per launch of a step kernel from one ncu capture
+    (profiles/ncu_traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(path):
         return None
     try:
         with open(path) as f:
             d = json.load(f)
-        e = d.get(workload, {}).get(kernel)
+        e = d.get(workload, {}).get(precision, {}).get(kernel)
         return None if e is None else float(e["dram_bytes_per_launch"])
     except (ValueError, KeyError, TypeError):
         return None
@@ -393,7 +395,7 @@ def run_ours(args, cp, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(ach / peak, 4),
-                     "traffic": load_traffic(name, dom),
+                     "traffic": load_traffic(name, args.precision, dom),
                      "peak_source": f"{peak_kind} hbm_gbs (STREAM copy; the only HBM figure "
                                     "measured)",
                      "algorithmic_bytes_per_launch": kernels[dom][1],

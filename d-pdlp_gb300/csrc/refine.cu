@@ -197,6 +197,7 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   Q.tile = P.tile;
   Q.A = P.A;
   Q.AT = P.AT;
+  Q.shape_key = P.shape_key;  // same structure: the rounds run round 0's kernels
   Q.c = c2;
   Q.lv = lv2;
   Q.uv = uv2;
@@ -262,7 +263,13 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
       launches += 2;
     }
     pdhg_parameters_t pi = params;
-    pi.termination_criteria.iteration_limit = (int)std::max<long>(0, limit - iters);
+    // the FP32 rounds leave 3 evaluation periods of the iteration limit to
+    // the FP64 finish: its infeasibility window (the first 3 periods, as in
+    // the reference's loop, src/solver.cu:62-65) certifies rays at
+    // eps_infeasible, which FP32 iterates cannot resolve
+    const long reserve = std::min<long>(3L * std::max(1, params.termination_evaluation_frequency),
+                                        limit / 2);
+    pi.termination_criteria.iteration_limit = (int)std::max<long>(0, limit - iters - reserve);
     double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     pi.termination_criteria.time_sec_limit = params.termination_criteria.time_sec_limit - elapsed;
     if (round > 0) {
@@ -377,6 +384,7 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
     W.tile = P.tile;
     W.A = P.A;
     W.AT = P.AT;
+    W.shape_key = P.shape_key;
     W.c = P.c;
     W.lv = P.lv;
     W.uv = P.uv;

@@ -172,6 +172,35 @@ int kernel_override() {
   return v;
 }
 
+namespace {
+std::mutex g_choice_mu;
+std::map<uint64_t, std::array<int, 2>> g_choice[3];
+
+uint64_t fnv1a(uint64_t h, const int *v, size_t count) {
+  for (size_t i = 0; i < count; ++i) {
+    uint32_t u = (uint32_t)v[i];
+    for (int b = 0; b < 4; ++b, u >>= 8) h = (h ^ (u & 0xffu)) * 1099511628211ull;
+  }
+  return h;
+}
+}  // namespace
+
+bool lookup_kernel_choice(uint64_t key, int prec, int c[2]) {
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  auto it = g_choice[prec].find(key);
+  if (it == g_choice[prec].end()) return false;
+  c[0] = it->second[0];
+  c[1] = it->second[1];
+  return true;
+}
+
+void settle_kernel_choice(uint64_t key, int prec, int c[2]) {
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  auto it = g_choice[prec].emplace(key, std::array<int, 2>{c[0], c[1]}).first;
+  c[0] = it->second[0];
+  c[1] = it->second[1];
+}
+
 DevProblem::~DevProblem() {
   if (arena) dev_free(arena, owner);
 }
@@ -207,6 +236,12 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
     const int *cj = prob->constraint_matrix_col_indices;
     for (int k = 0; k < nnz; ++k) tp[(size_t)cj[k] + 1]++;
     for (int c = 0; c < n; ++c) tp[c + 1] += tp[c];
+  }
+  {
+    const int dims[3] = {m, n, nnz};
+    uint64_t h = fnv1a(1469598103934665603ull, dims, 3);
+    h = fnv1a(h, prob->constraint_matrix_row_pointers, (size_t)m + 1);
+    P->shape_key = fnv1a(h, tp.data(), (size_t)n + 1);
   }
   std::vector<int4> blkA, blkT;
   std::vector<int2> lrA, lrT;

@@ -161,15 +161,26 @@ struct DevProblem {
   // return only after their work on the problem has finished.
   cudaStream_t owner = cudaStreamPerThread;
   // SpMV kernel per matrix and precision (index: 0 FP64, 1 FP32, 2 FP32
-  // matrix), measured by the first solve of each precision: -1 not yet
-  // measured, 0 fused, 1 pipelined; {A, A^T}
+  // matrix), chosen by the first solve of each precision: -1 not yet
+  // chosen, 0 fused, 1 pipelined; {A, A^T}
   mutable int kernel_choice[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+  // fingerprint of the structure the kernel choice depends on: m, n, nnz
+  // and the row lengths of A and A^T (FNV-1a over both row-pointer arrays)
+  uint64_t shape_key = 0;
   mutable std::mutex tune_mu;
   ~DevProblem();
 };
 
 // Validate, transpose (host), plan and upload.  Throws on a malformed CSR.
 DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st);
+
+// Kernel choices of this process by structure fingerprint and precision
+// index: every problem of one structure runs the kernels the first timed
+// solve of that structure chose.  lookup fills c and returns true when a
+// choice is recorded; settle records c unless one is already recorded, and
+// returns the recorded choice in c.
+bool lookup_kernel_choice(uint64_t key, int prec, int c[2]);
+void settle_kernel_choice(uint64_t key, int prec, int c[2]);
 
 // KKT measures of a point, in the reference's definitions.
 struct Kkt {

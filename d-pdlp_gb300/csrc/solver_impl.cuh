@@ -624,12 +624,19 @@ void Solve<T, M>::apply_kernels(bool pipe_A, bool pipe_T) {
   pw_.nlongA = d.nlongA;
 }
 
-// The SpMV kernel of each matrix, measured once per problem and precision:
-// the step kernel of the matrix (primal step over A^T, dual step over A) on
-// both kernels, 2 warm and 5 timed launches each, CUDA events on the solve's
-// stream; the pipelined kernel is kept where it is at least 3% faster.
-// Runs before the first iteration (the step kernels only write the next
-// iterates and x_ref, which the loop writes before it reads them).
+// The SpMV kernel of each matrix, chosen once per problem and precision.
+// Below kTuneMinNnz non-zeros both matrices take the fused kernel (launches
+// of a few microseconds, where it is never slower).  Above, the step kernel
+// of each matrix (primal step over A^T, dual step over A) is timed on both
+// kernels, 2 warm and 5 timed launches each, CUDA events on the solve's
+// stream, and the pipelined kernel is kept where it is at least 3% faster.
+// The choice is recorded for the structure (settle_kernel_choice), so every
+// later solve of a matrix of that structure in the process runs the same
+// kernels and returns the same bits.  Runs before the first iteration (the
+// step kernels only write the next iterates and x_ref, which the loop
+// writes before it reads them).
+constexpr long kTuneMinNnz = 1L << 22;
+
 template <class T, class M>
 void Solve<T, M>::tune_kernels() {
   if (tuned_) return;
@@ -637,36 +644,41 @@ void Solve<T, M>::tune_kernels() {
   std::lock_guard<std::mutex> lk(P_.tune_mu);
   int *ch = P_.kernel_choice[precision_index()];
   if (ch[0] < 0 || ch[1] < 0) {
-    Dev<T> &d = d_;
-    cudaEvent_t e0, e1;
-    PDLP_CUDA(cudaEventCreate(&e0));
-    PDLP_CUDA(cudaEventCreate(&e1));
-    auto timed = [&](auto &&launch) {
-      for (int i = 0; i < 2; ++i) launch();
-      PDLP_CUDA(cudaEventRecord(e0, st_));
-      for (int i = 0; i < 5; ++i) launch();
-      PDLP_CUDA(cudaEventRecord(e1, st_));
-      PDLP_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      PDLP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      return ms;
-    };
-    PrimalEpi<T, M, false, false, true> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
-    DualEpi<T, M, false, false, true> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
-    float tf[2] = {0.f, 0.f}, tp[2] = {0.f, 0.f};
-    for (int k = 0; k < 2; ++k) {
-      apply_kernels(k != 0, k != 0);
-      float a = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
-      float t = timed([&] { launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_); });
-      (k ? tp : tf)[0] = a;
-      (k ? tp : tf)[1] = t;
+    if (P_.nnz < kTuneMinNnz) {
+      ch[0] = ch[1] = 0;
+    } else if (!lookup_kernel_choice(P_.shape_key, precision_index(), ch)) {
+      Dev<T> &d = d_;
+      cudaEvent_t e0, e1;
+      PDLP_CUDA(cudaEventCreate(&e0));
+      PDLP_CUDA(cudaEventCreate(&e1));
+      auto timed = [&](auto &&launch) {
+        for (int i = 0; i < 2; ++i) launch();
+        PDLP_CUDA(cudaEventRecord(e0, st_));
+        for (int i = 0; i < 5; ++i) launch();
+        PDLP_CUDA(cudaEventRecord(e1, st_));
+        PDLP_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PDLP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+      };
+      PrimalEpi<T, M, false, false, true> pe{d, 0, d.x[0], d.y[0], d.x[1], T(0), T(0), T(0)};
+      DualEpi<T, M, false, false, true> de{d, 0, d.y[0], d.y[1], T(0), T(0), T(0), T(0)};
+      float tf[2] = {0.f, 0.f}, tp[2] = {0.f, 0.f};
+      for (int k = 0; k < 2; ++k) {
+        apply_kernels(k != 0, k != 0);
+        float a = timed([&] { launch_spmv(A_, de, d.p_dstep, d.lp_dstep, st_); });
+        float t = timed([&] { launch_spmv(AT_, pe, d.p_pstep, d.lp_pstep, st_); });
+        (k ? tp : tf)[0] = a;
+        (k ? tp : tf)[1] = t;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      ch[0] = P_.A.pipe.ntile > 0 && tp[0] < 0.97f * tf[0] ? 1 : 0;
+      ch[1] = P_.AT.pipe.ntile > 0 && tp[1] < 0.97f * tf[1] ? 1 : 0;
+      settle_kernel_choice(P_.shape_key, precision_index(), ch);
+      tune_ms_[0] = tf[0] / 5; tune_ms_[1] = tp[0] / 5;
+      tune_ms_[2] = tf[1] / 5; tune_ms_[3] = tp[1] / 5;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ch[0] = P_.A.pipe.ntile > 0 && tp[0] < 0.97f * tf[0] ? 1 : 0;
-    ch[1] = P_.AT.pipe.ntile > 0 && tp[1] < 0.97f * tf[1] ? 1 : 0;
-    tune_ms_[0] = tf[0] / 5; tune_ms_[1] = tp[0] / 5;
-    tune_ms_[2] = tf[1] / 5; tune_ms_[3] = tp[1] / 5;
   }
   apply_kernels(ch[0] != 0, ch[1] != 0);
 }

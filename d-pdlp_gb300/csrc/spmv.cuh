@@ -179,13 +179,18 @@ struct pre_of<E, true> {
 // register-path variant holds a group's columns and values across the first
 // barrier and runs at 5 blocks (48 registers; no spills in the dual-step
 // instantiation, 16 bytes in the primal-step one).
-template <int TILE, bool DIRECT = false>
+// FP32 values (PDLP_FUSED_FP32_BLOCKS, default 6) may run more blocks.
+#ifndef PDLP_FUSED_FP32_BLOCKS
+#define PDLP_FUSED_FP32_BLOCKS 6
+#endif
+template <int TILE, bool DIRECT = false, int VBYTES = 8>
 constexpr int spmv_min_blocks() {
-  return TILE >= 2048 ? 1 : DIRECT ? 5 : 6;
+  return TILE >= 2048 ? 1 : DIRECT ? 5 : VBYTES == 4 ? PDLP_FUSED_FP32_BLOCKS : 6;
 }
 
 template <int TILE, class Epi, bool DIRECT = false>
-__global__ void __launch_bounds__(kThreads, spmv_min_blocks<TILE, DIRECT>())
+__global__ void __launch_bounds__(kThreads,
+                                  spmv_min_blocks<TILE, DIRECT, sizeof(typename Epi::val_t)>())
     spmv_fused(const int *__restrict__ ptr, const int *__restrict__ col,
                const typename Epi::val_t *__restrict__ val, SpmvPlan plan,
                double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
