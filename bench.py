@@ -347,10 +347,22 @@ def run_ours(args, cp, rank, world, local):
             a, b = last.result, f_last.result
             rel = lambda u, v: abs(u - v) / (1.0 + abs(v))
             vrel = lambda u, v: float(abs(u - v).max() / (1.0 + abs(v).max())) if len(v) else 0.0
-            fp64["error_of_headline_vs_fp64"] = {
+            err = lambda a, b: {
                 "primal_obj_rel": rel(a["primal_objective_value"], b["primal_objective_value"]),
                 "dual_obj_rel": rel(a["dual_objective_value"], b["dual_objective_value"]),
                 "x_rel_max": vrel(a["x"], b["x"]), "y_rel_max": vrel(a["y"], b["y"])}
+            fp64["error_of_headline_vs_fp64"] = err(a, b)
+            if args.fp64_oracle_eps:
+                # untimed FP64 solve to a tighter tolerance: the FP64 oracle
+                # of the result (the configured mixed-precision comparison)
+                op = params_for(cp, args.fp64_oracle_eps)
+                oo = dp.solve(op, precision=cp.PRECISION_FP64)
+                fp64["oracle"] = {
+                    "eps": args.fp64_oracle_eps, "status": oo.result["status"],
+                    "iterations": oo.result["total_count"],
+                    "seconds": round(oo.info["device_seconds"], 3),
+                    "error_of_headline": err(a, oo.result),
+                    "error_of_fp64": err(b, oo.result)}
     clocks = clk.summary()
     value, e2e_mean = max_over_ranks([statistics.mean(dev_s), statistics.mean(e2e_s)])
     r = last.result
@@ -798,6 +810,9 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="time the iteration kernels alone and exit (a short command for "
                          "profilers; prints no bench line)")
+    ap.add_argument("--fp64-oracle-eps", type=float, default=0.0,
+                    help="also solve the LP in FP64 to this tolerance (untimed) and report "
+                         "the error of the headline and FP64 results against it")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed FP64 solves reported beside an FP32 run (0: skip)")
     args = ap.parse_args()

@@ -173,19 +173,28 @@ struct pre_of<E, true> {
 
 // Resident blocks per SM the register allocation must allow.  The kernel is
 // latency-bound (dependent col -> gather -> FMA chains, per-row vector loads),
-// so residency pays: 6 blocks of 256 threads (40 registers) for tiles of up
-// to 1024 non-zeros.  2048-element tiles need their registers (the long-row
-// path keeps 8 loads per thread in flight) and run at 4 blocks.  The
-// register-path variant holds a group's columns and values across the first
-// barrier and runs at 5 blocks (48 registers; no spills in the dual-step
-// instantiation, 16 bytes in the primal-step one).
-// FP32 values (PDLP_FUSED_FP32_BLOCKS, default 6) may run more blocks.
+// so residency pays: 6 blocks of 256 threads (40 registers) for FP64 tiles of
+// up to 1024 non-zeros, 8 blocks (32 registers, up to 28 bytes of L1-resident
+// spills) for FP32 values -- measured on GB300 against 6 blocks: the 20M-nnz
+// power-law primal step 0.115 -> 0.102 ms, the transport primal step 0.163
+// -> 0.131 ms and its dual step 0.079 -> 0.073 ms.  2048-element tiles need
+// their registers (the long-row path keeps 8 loads per thread in flight) and
+// run at 4 blocks.  The register-path variant holds a group's columns and
+// values across the first barrier and runs at 5 blocks (48 registers).
+// PDLP_FUSED_FP32_BLOCKS and PDLP_DIRECT_FP32_BLOCKS override the FP32 counts
+// at build time.
 #ifndef PDLP_FUSED_FP32_BLOCKS
-#define PDLP_FUSED_FP32_BLOCKS 6
+#define PDLP_FUSED_FP32_BLOCKS 8
+#endif
+#ifndef PDLP_DIRECT_FP32_BLOCKS
+#define PDLP_DIRECT_FP32_BLOCKS 5
 #endif
 template <int TILE, bool DIRECT = false, int VBYTES = 8>
 constexpr int spmv_min_blocks() {
-  return TILE >= 2048 ? 1 : DIRECT ? 5 : VBYTES == 4 ? PDLP_FUSED_FP32_BLOCKS : 6;
+  return TILE >= 2048 ? 1
+         : DIRECT     ? (VBYTES == 4 ? PDLP_DIRECT_FP32_BLOCKS : 5)
+         : VBYTES == 4 ? PDLP_FUSED_FP32_BLOCKS
+                       : 6;
 }
 
 template <int TILE, class Epi, bool DIRECT = false>
