@@ -531,6 +531,10 @@ def run_batch(args, cp):
                    <= 10 * args.eps * (1 + abs(b["primal_objective_value"]))
                    for a, b in zip(res, seq))
     value = statistics.mean(vals)
+    # work done: non-zeros x iterations summed over the LPs (one iteration
+    # is one pass over A and one over A^T), as a rate against each path's time
+    nnz_it = sum(sh[2] * r["total_count"] for sh, r in zip(shapes, res) if r is not None)
+    nnz_it_seq = sum(sh[2] * r["total_count"] for sh, r in zip(shapes, seq) if r is not None)
     # the reference's own single-GPU FP64 solve, LP after LP in batch order
     # (a fresh process each), for about a minute: sequential LPs/s
     ref_seq = None
@@ -581,9 +585,13 @@ def run_batch(args, cp):
                 "d2h_bytes_per_step": int(sum(8 * (2 * sh[1] + sh[0]) for sh in shapes)),
                 "api": "pdlp_batch_solve from host arrays (upload, solve, copy-back per LP)"},
         "sequential": {"lps_per_second": round(count / t_seq, 2), "seconds": round(t_seq, 2),
+                       "nnz_iterations": nnz_it_seq,
+                       "g_nnz_iterations_per_s": round(nnz_it_seq / t_seq / 1e9, 2),
                        "api": "solve_lp_problem, one LP after another"},
         "reference_sequential": ref_seq,
-        "batch": {"iterations": iters, "failed": failed, "max_concurrent": info["max_concurrent"],
+        "batch": {"iterations": iters, "nnz_iterations": nnz_it,
+                  "g_nnz_iterations_per_s": round(nnz_it * value / count / 1e9, 2),
+                  "failed": failed, "max_concurrent": info["max_concurrent"],
                   "statuses": statuses, "worst_relative_kkt": worst,
                   "results_match_sequential": same},
         "fp64_batched": fp64_batch,

@@ -170,6 +170,7 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
     W->pipe.lcnt = (unsigned *)take((size_t)W->pipe.nlong * 4);
     W->pipe.lsum = (double *)take((size_t)W->pipe.ntile * 8);
     W->pipe.err = (int *)take(4);
+    W->plan.err = W->pipe.err;
     if (W->pipe.nlong)
       PDLP_CUDA(cudaMemsetAsync(W->pipe.lcnt, 0, (size_t)W->pipe.nlong * 4, st));
     PDLP_CUDA(cudaMemsetAsync(W->pipe.err, 0, sizeof(int), st));

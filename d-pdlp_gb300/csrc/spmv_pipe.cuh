@@ -81,7 +81,6 @@ static_assert(kPipeStageBytes - kPipeTileBytes >= kThreads * 8 &&
               "lane-sum area of a stage");
 constexpr int kPipeStages = PDLP_PIPE_STAGES;
 constexpr int kPipeCtasPerSm = PDLP_PIPE_CTAS;
-constexpr long long kPipeWaitCycles = 4000000000LL;  // ~2 s at 2 GHz, then give up
 
 // Byte layout of one tile in a stage buffer: row pointers [r0, r1], columns
 // and values [k0, k1), NV vectors [r0, r1); each range widened to 16-byte
@@ -165,62 +164,12 @@ inline void build_pipe_plan_host(int rows, const int *ptr, int NV, std::vector<i
   }
 }
 
-// ---------------------------------------------------------------- PTX
-__device__ __forceinline__ uint32_t smem_addr(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// L2 policy for data read once per sweep (the tile streams): evicted first,
-// so the gathered iterate vectors (8-80 MB) stay resident in the 129 MB L2
-// while ~0.5 GB of matrix streams through it every iteration.
-__device__ __forceinline__ uint64_t l2_evict_first() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         uint64_t *bar, uint64_t pol) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
-      "[%0], [%1], %2, [%3], %4;" ::"r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
-      : "memory");
-}
 // ticket of a long row's chunk: counts the arrival after this thread's
 // earlier writes (the chunk sum) are visible; returns the previous count
 __device__ __forceinline__ unsigned ticket_release(unsigned *p) {
   unsigned prev;
   asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(p) : "memory");
   return prev;
-}
-
-// Bounded wait for a stage: false after kPipeWaitCycles without completion.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > kPipeWaitCycles) return false;
-  return true;
 }
 
 // Per-lane accumulation of a run of products.  FP64 matrices: one FMA per
@@ -268,19 +217,6 @@ struct LaneAcc<float> {
   __device__ __forceinline__ float rounded() const { return __fadd_rn(h, l); }
 };
 
-// Epilogues that stage per-row vectors declare NV, vec_t, vecs and make_pre;
-// the others read their vectors from global memory in row().
-template <class E, class = void>
-struct pipe_vectors {
-  static constexpr int NV = 0;
-  using vec_t = double;
-};
-template <class E>
-struct pipe_vectors<E, std::void_t<decltype(E::NV)>> {
-  static constexpr int NV = E::NV;
-  using vec_t = typename E::vec_t;
-};
-
 // The pipelined step kernel's plan (per matrix): tiles, long rows, grid.
 struct PipePlan {
   int ntile = 0, nlong = 0, grid = 0;
@@ -326,9 +262,9 @@ __global__ void __launch_bounds__(kPipeBlock, kPipeCtasPerSm)
               double *__restrict__ part, double *__restrict__ lpart, Epi epi) {
   using M = typename Epi::val_t;
   using A = typename Epi::acc_t;
-  using T = typename pipe_vectors<Epi>::vec_t;
+  using T = typename step_vectors<Epi>::vec_t;
   constexpr int NF = Epi::NF;
-  constexpr int NV = pipe_vectors<Epi>::NV;
+  constexpr int NV = step_vectors<Epi>::NV;
   static_assert(sizeof(A) == sizeof(M), "run partials share the value buffer");
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[kPipeStages];
