@@ -12,6 +12,12 @@
 // its termination test uses the original's bound / objective norms.  FP32
 // only has to represent the correction, which shrinks round after round.
 // Residuals, corrections and the final KKT are FP64 throughout.
+//
+// Tolerances below 1e-4: round 0 stops at a relaxed tolerance (30 x eps,
+// within [1e-5, 1e-4]) and an FP64 PDHG solve warm-started at the FP64 point
+// with a cold primal weight (the FP64 finish) completes the solve; the
+// correction rounds then serve the cases where round 0 stalls above it.
+// Every path ends with the FP64 finish when the rounds miss the tolerance.
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -170,7 +176,6 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
     W->pipe.lcnt = (unsigned *)take((size_t)W->pipe.nlong * 4);
     W->pipe.lsum = (double *)take((size_t)W->pipe.ntile * 8);
     W->pipe.err = (int *)take(4);
-    W->plan.err = W->pipe.err;
     if (W->pipe.nlong)
       PDLP_CUDA(cudaMemsetAsync(W->pipe.lcnt, 0, (size_t)W->pipe.nlong * 4, st));
     PDLP_CUDA(cudaMemsetAsync(W->pipe.err, 0, sizeof(int), st));
@@ -242,6 +247,16 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
   reason = TERMINATION_REASON_ITERATION_LIMIT;  // unless a round meets the tolerances
   cupdlpx_result_t *ray_result = nullptr;
   double rescale_sec = 0.0;
+  // Round 0's tolerance.  Below 1e-4, FP32 runs only the first part of the
+  // way: to 30 x eps (at least 1e-5, at most 1e-4), where FP32 iterates are
+  // still reliable, and the FP64 finish below takes the point the rest of
+  // the way.  Measured on the 20M-nnz transport LP at eps 1e-6 (GB300): FP32
+  // to 3e-5 (28,600 iterations) then 9,300 FP64 iterations, 9.3 s, against
+  // 29.4 s for FP64 alone (100,600 iterations); FP32 alone stalls near 5e-6
+  // (197,000 iterations), and correction rounds from the 1e-5 point cost
+  // more than they gained.
+  const double eps_min = fmin(eps_feas, eps_opt);
+  const double eps0 = eps_min < 1e-4 ? fmin(1e-4, fmax(30.0 * eps_min, 1e-5)) : 0.0;
   for (int round = 0; round < opt.max_rounds; ++round) {
     const DevProblem &R = round == 0 ? P : Q;
     bool stop = false;
@@ -264,6 +279,10 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
       launches += 2;
     }
     pdhg_parameters_t pi = params;
+    if (round == 0 && eps0 > 0.0) {
+      pi.termination_criteria.eps_feasible_relative = fmax(eps_feas, eps0);
+      pi.termination_criteria.eps_optimal_relative = fmax(eps_opt, eps0);
+    }
     // the FP32 rounds leave 3 evaluation periods of the iteration limit to
     // the FP64 finish: its infeasibility window (the first 3 periods, as in
     // the reference's loop, src/solver.cu:62-65) certifies rays at
@@ -357,6 +376,8 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
         reason = r == TERMINATION_REASON_TIME_LIMIT ? r : TERMINATION_REASON_ITERATION_LIMIT;
         return true;
       }
+      // round 0 met its relaxed tolerance: the FP64 finish takes it from here
+      if (round == 0 && eps0 > 0.0 && r == TERMINATION_REASON_OPTIMAL) return true;
       return weak;
     };
     if (opt.fp64_iterates) {
@@ -403,7 +424,11 @@ cupdlpx_result_t *solve_refined(const DevProblem &P, const pdhg_parameters_t &pa
     pf.termination_criteria.time_sec_limit = left_sec;
     Solve<double> s(pf, st, W, 0);
     s.prepare();
-    s.init_step(sigma, omega0);
+    // a cold primal weight: the FP32 rounds' weight has drifted under FP32
+    // noise in the distances it balances (the 20M transport LP at 1e-6: from
+    // a point at 2.3e-6, 220,200 FP64 iterations with round 0's weight
+    // 1.5e-6, 4,200 with the cold one)
+    s.init_step(sigma, 0.0);
     s.run();
     iters += s.total_count();
     launches += s.kernel_launches();

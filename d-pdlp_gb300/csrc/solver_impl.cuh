@@ -508,7 +508,6 @@ void Solve<T, M>::alloc() {
     W.pipe.lcnt = ar.take<unsigned>(S.pipe.nlong);
     W.pipe.lsum = ar.take<double>(S.pipe.ntile);
     W.pipe.err = ar.take<int>(1);
-    W.plan.err = W.pipe.err;  // one flag for both kernels' copy timeouts
     if (S.pipe.nlong) PDLP_CUDA(cudaMemsetAsync(W.pipe.lcnt, 0, (size_t)S.pipe.nlong * 4, st_));
     PDLP_CUDA(cudaMemsetAsync(W.pipe.err, 0, sizeof(int), st_));
   };
@@ -1123,9 +1122,8 @@ void Solve<T, M>::run() {
   check_pipe_errors();
 }
 
-// A copy wait of an SpMV kernel that timed out leaves a flag (a stage of the
-// pipelined kernel, or the staged row vectors of the fused kernel's FP32
-// steps); the iterates are then not to be trusted.
+// A stage wait of the pipelined kernel that timed out leaves a flag (the
+// kernel then stopped early, so the iterates are not to be trusted).
 template <class T, class M>
 void Solve<T, M>::check_pipe_errors() const {
   int e[2] = {0, 0};
@@ -1134,7 +1132,7 @@ void Solve<T, M>::check_pipe_errors() const {
     if (flags[i]) PDLP_CUDA(cudaMemcpyAsync(&e[i], flags[i], sizeof(int), cudaMemcpyDeviceToHost, st_));
   PDLP_CUDA(cudaStreamSynchronize(st_));
   if (e[0] || e[1])
-    throw std::runtime_error("SpMV: a bulk copy did not complete within its wait limit");
+    throw std::runtime_error("pipelined SpMV: a tile copy did not complete within its wait limit");
 }
 
 // finite entries -> 0 (the dual feasibility problem's bounds)

@@ -35,7 +35,6 @@
 #include <type_traits>
 #include <vector>
 
-#include "bulk.cuh"
 #include "common.cuh"
 
 namespace pdlp {
@@ -49,7 +48,6 @@ struct SpmvPlan {
   int2 *lrow = nullptr;       // per long row {first block, chunk count}
   unsigned *lcnt = nullptr;   // per long row arrival counter (kept at 0)
   double *lsum = nullptr;     // per block chunk partial (long rows)
-  int *err = nullptr;         // per solve: set when a vector copy timed out
 };
 
 // Host: cut rows into tiles.  `ptr` is the host copy of the row pointer.
@@ -201,26 +199,6 @@ constexpr int spmv_min_blocks() {
                        : 6;
 }
 
-// Per-row vectors of a light tile by bulk copy.  A step epilogue with 4-byte
-// vectors (the FP32 solve's primal and dual steps) on the staged kernel gets
-// the tile's ranges [r0, r1) of its NV vectors (x, c, bounds, anchor; or y,
-// bounds, anchor) copied to shared memory by one thread at block start, one
-// cp.async.bulk each, completion counted on an mbarrier, while the block
-// streams the matrix; the row fold then reads them from shared memory.  With
-// register preloads only each thread's first row had its vectors in flight,
-// and a tile of more than 256 rows (1-4 non-zeros a row: most of a power-law
-// LP's A^T) waited on one more dependent round of loads.  Tiles of more than
-// kStageRows rows keep the register path.  Ranges widen to 16-byte copy
-// boundaries; the arrays are 256-byte-aligned allocations padded to 256
-// bytes, so the widened copies stay inside them.
-constexpr int kStageRows = 512;
-constexpr int kStageStride = kStageRows + 8;  // elements per staged vector
-
-template <class Epi, bool DIRECT>
-constexpr bool stages_vectors() {
-  return !DIRECT && step_vectors<Epi>::NV > 0 && sizeof(typename step_vectors<Epi>::vec_t) == 4;
-}
-
 template <int TILE, class Epi, bool DIRECT = false>
 __global__ void __launch_bounds__(kThreads,
                                   spmv_min_blocks<TILE, DIRECT, sizeof(typename Epi::val_t)>())
@@ -239,33 +217,12 @@ __global__ void __launch_bounds__(kThreads,
   __shared__ double red[8 * (NF > 0 ? NF : 1) + 8];
   __shared__ double sc[4];
   __shared__ int s_last;
-  constexpr bool SV = stages_vectors<Epi, DIRECT>();
-  using VT = typename step_vectors<Epi>::vec_t;
-  constexpr int NVS = SV ? step_vectors<Epi>::NV : 1;
-  __shared__ __align__(16) VT svec[SV ? NVS * kStageStride : 4];
-  __shared__ __align__(8) uint64_t vbar;
 
   if (!epi.init()) return;
   if (threadIdx.x == 0) epi.prologue(sc);
   const int4 b = plan.blk[blockIdx.x];
   const int k0 = b.z, len = b.w - b.z;
   const int R = b.y >= 0 ? b.y - b.x : 0;
-  // staged-vector tile (block-uniform): light, short rows, at most kStageRows
-  const bool stagev = SV && R > 1 && len <= 64 * R && R <= kStageRows;
-  const int va = b.x & ~3;  // first vector element copied
-  if constexpr (SV) {
-    if (stagev && threadIdx.x == 0) {
-      const unsigned bytes = (unsigned)((((b.y + 3) & ~3) - va) * 4);
-      mbar_init(&vbar, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      mbar_arrive_expect_tx(&vbar, bytes * NVS);
-      const VT *vp[NVS];
-      epi.vecs(vp);
-      const uint64_t pol = l2_evict_first();
-#pragma unroll
-      for (int q = 0; q < NVS; ++q) bulk_g2s(svec + q * kStageStride, vp[q] + va, bytes, &vbar, pol);
-    }
-  }
   double acc[NF > 0 ? NF : 1];
 #pragma unroll
   for (int f = 0; f < (NF > 0 ? NF : 1); ++f) acc[f] = 0.0;
@@ -461,7 +418,7 @@ __global__ void __launch_bounds__(kThreads,
         }
       }
       if constexpr (has_preload<Epi>::value) {
-        if (stream && !stagev && threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
+        if (stream && threadIdx.x < R) epi.preload(b.x + threadIdx.x, pre);
       }
       for (int j = threadIdx.x; j <= R; j += kThreads) soff[j] = ptr[b.x + j] - k0;
 #pragma unroll
@@ -502,11 +459,6 @@ __global__ void __launch_bounds__(kThreads,
         sv[swz<T>(segs)] = (T)s;
       }
       __syncthreads();
-      if constexpr (SV) {
-        // every thread waits (bounded), so none leaves with copies in flight
-        if (stagev && !mbar_wait_bounded(&vbar, 0) && threadIdx.x == 0 && plan.err)
-          atomicOr(plan.err, 2);
-      }
       // Row fold: segment at the row start, then one per lane boundary inside.
       for (int j = threadIdx.x; j < R; j += kThreads) {
         const int a = soff[j], e = soff[j + 1];
@@ -514,15 +466,6 @@ __global__ void __launch_bounds__(kThreads,
         if (a < e) {
           sum = (A)sv[swz<T>(a)];
           for (int q = (a / SEG + 1) * SEG; q < e; q += SEG) sum += (A)sv[swz<T>(q)];
-        }
-        if constexpr (SV) {
-          if (stagev) {
-            VT v[NVS];
-#pragma unroll
-            for (int q = 0; q < NVS; ++q) v[q] = svec[q * kStageStride + (b.x - va) + j];
-            epi.row_pre(b.x + j, sum, epi.make_pre(v), acc);
-            continue;
-          }
         }
         if constexpr (has_preload<Epi>::value) {
           if (j == (int)threadIdx.x) epi.row_pre(b.x + j, sum, pre, acc);

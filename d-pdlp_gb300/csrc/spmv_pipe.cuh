@@ -49,6 +49,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "bulk.cuh"
 #include "spmv.cuh"
 
 namespace pdlp {
