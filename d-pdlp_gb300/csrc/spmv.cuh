@@ -180,16 +180,19 @@ struct pre_of<E, true> {
 // -> 0.131 ms and its dual step 0.079 -> 0.073 ms.  2048-element tiles need
 // their registers (the long-row path keeps 8 loads per thread in flight) and
 // run at 4 blocks.  The register-path variant holds a group's columns and
-// values across the first barrier and runs at 5 blocks (48 registers) in
-// FP64, 8 in FP32 (32 registers, up to 32 bytes of spills; the power-law
-// dual step 0.107 ms at 5 blocks, 0.098 at 6, 0.093 at 8).
+// values across the first barrier and runs at 5 blocks (48 registers).  In
+// FP32 it is faster at 8 (the power-law dual step 0.107 ms at 5 blocks, 0.093
+// at 8), but then the per-matrix choice on the 20M-nnz power-law LP takes it
+// for A instead of the pipelined kernel, and with its rounding that LP's FP32
+// trajectory needs 69,400 iterations to 1e-4 against 55,200: 14.4 s against
+// 11.5 s end to end, so 5 stays the default.
 // PDLP_FUSED_FP32_BLOCKS and PDLP_DIRECT_FP32_BLOCKS override the FP32 counts
 // at build time.
 #ifndef PDLP_FUSED_FP32_BLOCKS
 #define PDLP_FUSED_FP32_BLOCKS 8
 #endif
 #ifndef PDLP_DIRECT_FP32_BLOCKS
-#define PDLP_DIRECT_FP32_BLOCKS 8
+#define PDLP_DIRECT_FP32_BLOCKS 5
 #endif
 template <int TILE, bool DIRECT = false, int VBYTES = 8>
 constexpr int spmv_min_blocks() {
