@@ -540,7 +540,7 @@ def run_batch(args, cp):
     ref_seq = None
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    if oracle_lib.ref_gpu_available() and gpu_visible():
+    if oracle_lib.ref_gpu_available() and gpu_visible() and args.ref_seconds > 0:
         t0, k, solve_s = time.perf_counter(), 0, 0.0
         try:
             while k < count and time.perf_counter() - t0 < args.ref_seconds:

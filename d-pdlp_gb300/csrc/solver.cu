@@ -7,6 +7,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <exception>
 #include <thread>
 
 #include "solver_impl.cuh"
@@ -176,12 +178,31 @@ namespace {
 std::mutex g_choice_mu;
 std::map<uint64_t, std::array<int, 2>> g_choice[3];
 
+// FNV-1a over 32-bit words (the fingerprint only has to separate structures
+// within one process)
 uint64_t fnv1a(uint64_t h, const int *v, size_t count) {
-  for (size_t i = 0; i < count; ++i) {
-    uint32_t u = (uint32_t)v[i];
-    for (int b = 0; b < 4; ++b, u >>= 8) h = (h ^ (u & 0xffu)) * 1099511628211ull;
-  }
+  for (size_t i = 0; i < count; ++i) h = (h ^ (uint32_t)v[i]) * 1099511628211ull;
   return h;
+}
+
+// Host threads for the upload's passes over the non-zeros (LPs of 2M+
+// non-zeros; smaller ones stay on the calling thread).
+int upload_threads(long nnz) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return nnz >= (1L << 21) ? (int)std::min(16u, hw ? hw : 1u) : 1;
+}
+
+// f(begin, end) over [0, count) in T contiguous slices, slice 0 on this thread
+template <class F>
+void parallel_slices(int T, long count, F &&f) {
+  if (T <= 1) {
+    f(0L, count);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) th.emplace_back([&f, t, T, count] { f(count * t / T, count * (t + 1) / T); });
+  f(0L, count / T);
+  for (auto &x : th) x.join();
 }
 }  // namespace
 
@@ -219,7 +240,17 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
               (m == 0 || (prob->constraint_lower_bound && prob->constraint_upper_bound));
     if (ok) ok = rp[0] == 0 && rp[m] == nnz;
     for (int r = 0; ok && r < m; ++r) ok = rp[r] <= rp[r + 1];
-    for (int k = 0; ok && k < nnz; ++k) ok = cj[k] >= 0 && cj[k] < n;
+    if (ok) {
+      std::atomic<bool> bad{false};
+      parallel_slices(upload_threads(nnz), nnz, [&](long a, long b) {
+        for (long k = a; k < b; ++k)
+          if (cj[k] < 0 || cj[k] >= n) {
+            bad.store(true, std::memory_order_relaxed);
+            return;
+          }
+      });
+      ok = !bad.load();
+    }
     if (!ok) throw std::runtime_error("invalid CSR matrix (row pointers or column indices)");
   }
   auto P = std::make_unique<DevProblem>();
@@ -234,7 +265,15 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   std::vector<int> tp((size_t)n + 1, 0);
   {
     const int *cj = prob->constraint_matrix_col_indices;
-    for (int k = 0; k < nnz; ++k) tp[(size_t)cj[k] + 1]++;
+    int *cnt = tp.data() + 1;
+    const int T = upload_threads(nnz);
+    if (T > 1) {
+      parallel_slices(T, nnz, [&](long a, long b) {
+        for (long k = a; k < b; ++k) __atomic_fetch_add(cnt + cj[k], 1, __ATOMIC_RELAXED);
+      });
+    } else {
+      for (int k = 0; k < nnz; ++k) cnt[cj[k]]++;
+    }
     for (int c = 0; c < n; ++c) tp[c + 1] += tp[c];
   }
   {
@@ -246,14 +285,36 @@ DevProblem *upload_problem(const lp_problem_t *prob, cudaStream_t st) {
   std::vector<int4> blkA, blkT;
   std::vector<int2> lrA, lrT;
   const int chunk = pick_chunk(P->tile);
-  build_plan_host(m, prob->constraint_matrix_row_pointers, P->tile, blkA, lrA, chunk);
-  build_plan_host(n, tp.data(), P->tile, blkT, lrT, chunk);
   // pipelined step kernel: the dual step (A) stages 4 row vectors, the
-  // primal step (A^T) 5
+  // primal step (A^T) 5.  A's plans are built on a second thread for large
+  // LPs, beside A^T's.
   std::vector<int4> pblkA, pblkT;
   std::vector<int2> plrA, plrT;
-  build_pipe_plan_host(m, prob->constraint_matrix_row_pointers, 4, pblkA, plrA);
-  build_pipe_plan_host(n, tp.data(), 5, pblkT, plrT);
+  auto plans_A = [&] {
+    build_plan_host(m, prob->constraint_matrix_row_pointers, P->tile, blkA, lrA, chunk);
+    build_pipe_plan_host(m, prob->constraint_matrix_row_pointers, 4, pblkA, plrA);
+  };
+  std::exception_ptr failed_A;
+  std::thread thread_A;
+  if (upload_threads(nnz) > 1)
+    thread_A = std::thread([&] {
+      try {
+        plans_A();
+      } catch (...) {
+        failed_A = std::current_exception();
+      }
+    });
+  else
+    plans_A();
+  try {
+    build_plan_host(n, tp.data(), P->tile, blkT, lrT, chunk);
+    build_pipe_plan_host(n, tp.data(), 5, pblkT, plrT);
+  } catch (...) {
+    if (thread_A.joinable()) thread_A.join();
+    throw;
+  }
+  if (thread_A.joinable()) thread_A.join();
+  if (failed_A) std::rethrow_exception(failed_A);
   int dev = 0, nsm = kNumSms;
   PDLP_CUDA(cudaGetDevice(&dev));
   PDLP_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
