@@ -1,6 +1,6 @@
 """FP32 PDHG with FP64 iterative refinement: the FP64 KKT of the original LP
 meets the requested tolerance and the objectives agree with the FP64 oracle
-(spec criterion: 1e-6 relative at tight tolerance)."""
+(the objective bar: 1e-6 relative at tight tolerance)."""
 import numpy as np
 import pytest
 

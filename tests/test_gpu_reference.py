@@ -26,7 +26,7 @@ import oracle_lib as ol
 
 pytestmark = pytest.mark.gpu
 
-OBJ_TOL = 1e-6      # spec bar on the primal and dual objectives
+OBJ_TOL = 1e-6      # bar on the primal and dual objectives at eps 1e-8
 VEC_TOL = 1e-7      # max |a - b| / (1 + max |b|) on x, y, reduced cost
 
 
