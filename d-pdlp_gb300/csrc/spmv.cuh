@@ -186,10 +186,15 @@ struct pre_of<E, true> {
 // for A instead of the pipelined kernel, and with its rounding that LP's FP32
 // trajectory needs 69,400 iterations to 1e-4 against 55,200: 14.4 s against
 // 11.5 s end to end, so 5 stays the default.
-// PDLP_FUSED_FP32_BLOCKS and PDLP_DIRECT_FP32_BLOCKS override the FP32 counts
-// at build time.
+// FP64 tiles stay at 6: at 8 (32 registers, 120 bytes of spills) the
+// power-law primal step goes from 0.153 to 0.183 ms, the FP64 pipe being
+// the other bound there.  PDLP_FUSED_FP32_BLOCKS, PDLP_DIRECT_FP32_BLOCKS and
+// PDLP_FUSED_FP64_BLOCKS override the counts at build time.
 #ifndef PDLP_FUSED_FP32_BLOCKS
 #define PDLP_FUSED_FP32_BLOCKS 8
+#endif
+#ifndef PDLP_FUSED_FP64_BLOCKS
+#define PDLP_FUSED_FP64_BLOCKS 6
 #endif
 #ifndef PDLP_DIRECT_FP32_BLOCKS
 #define PDLP_DIRECT_FP32_BLOCKS 5
@@ -199,7 +204,7 @@ constexpr int spmv_min_blocks() {
   return TILE >= 2048 ? 1
          : DIRECT     ? (VBYTES == 4 ? PDLP_DIRECT_FP32_BLOCKS : 5)
          : VBYTES == 4 ? PDLP_FUSED_FP32_BLOCKS
-                       : 6;
+                       : PDLP_FUSED_FP64_BLOCKS;
 }
 
 template <int TILE, class Epi, bool DIRECT = false>
